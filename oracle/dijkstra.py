@@ -1,0 +1,80 @@
+"""Oracle A7–A8: ROI heap Dijkstra and backtrace (CPU restatement).
+
+Reference: ``SimpleDijkstra.find_path_roi``
+(``orthoroute/algorithms/manhattan/unified_pathfinder.py:2451-2548``).
+
+Semantics kept exactly:
+
+* heap entries are ``(python float label, roi index)``; ties pop the lower
+  ROI index first;
+* ``dist`` is a float32 array: a relaxation ``alt = (du + float(cost)) +
+  float(pen[v])`` (FP64) is accepted iff ``alt < float(dist[v])``, then
+  ``dist[v] = float32(alt)``, ``parent[v] = u`` and ``alt`` is pushed;
+* each node is settled once; the search stops when dst is popped;
+* backtrace walks ``parent`` from dst and reverses; a single-node path is
+  ``None``.
+
+``find_path_roi_trace`` additionally returns the settled labels and the
+count of scanned arcs (the algorithmic edge count used for GTEPS).
+"""
+from __future__ import annotations
+
+import heapq
+from typing import List, Optional
+
+import numpy as np
+
+
+def find_path_roi(indptr, indices, src, dst, costs, roi_nodes, global_to_roi,
+                  node_penalty=None, stats=None) -> Optional[List[int]]:
+    roi_src = int(global_to_roi[src])
+    roi_dst = int(global_to_roi[dst])
+    if roi_src < 0 or roi_dst < 0:
+        return None
+    R = len(roi_nodes)
+    dist = np.full(R, np.inf, dtype=np.float32)
+    parent = np.full(R, -1, dtype=np.int32)
+    visited = np.zeros(R, dtype=bool)
+    dist[roi_src] = 0.0
+    heap = [(0.0, roi_src)]
+    # Python-level views for speed (same values as the numpy arrays).
+    ip = indptr.tolist() if hasattr(indptr, "tolist") else indptr
+    ix = indices
+    cst = costs
+    pen = node_penalty
+    scanned = 0
+    settled = 0
+    while heap:
+        du, u = heapq.heappop(heap)
+        if visited[u]:
+            continue
+        visited[u] = True
+        settled += 1
+        if u == roi_dst:
+            break
+        ug = int(roi_nodes[u])
+        s, e = ip[ug], ip[ug + 1]
+        for ei in range(s, e):
+            scanned += 1
+            vg = int(ix[ei])
+            v = int(global_to_roi[vg])
+            if v < 0 or visited[v]:
+                continue
+            alt = du + float(cst[ei])
+            if pen is not None:
+                alt += float(pen[v])
+            if alt < dist[v]:
+                dist[v] = alt
+                parent[v] = u
+                heapq.heappush(heap, (alt, v))
+    if stats is not None:
+        stats["scanned"] = stats.get("scanned", 0) + scanned
+        stats["settled"] = stats.get("settled", 0) + settled
+    if not np.isfinite(dist[roi_dst]):
+        return None
+    path, cur = [], roi_dst
+    while cur != -1:
+        path.append(int(roi_nodes[cur]))
+        cur = int(parent[cur])
+    path.reverse()
+    return path if len(path) > 1 else None

@@ -1,0 +1,12 @@
+"""Shared pytest configuration: the ``gpu`` marker and repo-root import path."""
+import os
+import sys
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA device (GB300, sm_103a)")
+    config.addinivalue_line("markers", "slow: long CPU-oracle runs")
