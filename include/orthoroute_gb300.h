@@ -1,0 +1,200 @@
+/*
+ * orthoroute_gb300 — C ABI of the GB300 (sm_103a) PathFinder hot path.
+ *
+ * Drop-in boundary for OrthoRoute's negotiated-congestion inner loop
+ * (orthoroute/algorithms/manhattan/unified_pathfinder.py).  Every entry point
+ * takes plain pointers and sizes; every device buffer is owned by the caller
+ * (the Python host allocates them as torch tensors and passes data_ptr()).
+ * Scratch memory is a caller-provided workspace whose size is queried first.
+ *
+ * Conventions
+ *   - return value: OGR_OK (0), OGR_NO_PATH (1) or a negative error;
+ *   - `stream` is a cudaStream_t passed as void* (NULL = legacy stream);
+ *   - no entry point synchronises the host unless it says so;
+ *   - float scalars are the float32 roundings numpy would apply to the
+ *     reference's Python floats (numpy 2 weak-scalar rule).
+ */
+#ifndef ORTHOROUTE_GB300_H
+#define ORTHOROUTE_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  OGR_OK = 0,
+  OGR_NO_PATH = 1,
+  OGR_ERR_ARG = -1,
+  OGR_ERR_CUDA = -2,
+  OGR_ERR_CAPACITY = -3,  /* a queue, ROI or path buffer is too small     */
+  OGR_ERR_ITER_CAP = -4,  /* a device loop reached its iteration limit     */
+  OGR_ERR_NUMERIC = -5    /* an input violated an exactness precondition  */
+};
+
+/* ------------------------------------------------------------------ A1 ---
+ * 3-D lattice → CSR.  Replaces Lattice3D.build_graph + CSRGraph.finalize
+ * (unified_pathfinder.py:1656-1955 and :881-1002).  Rows are sorted by
+ * destination id, exactly like the reference's structured sort
+ * (order='src' breaks ties on dst then cost, :935).
+ */
+typedef struct {
+  int32_t nx, ny, nz;
+  float lateral_cost;          /* float32(pitch)                            */
+  float wrong_way_cost;        /* <= 0: strict H/V discipline               */
+  const uint8_t* layer_axis;   /* host [nz]: 0 none, 1 'h', 2 'v'           */
+  const int32_t* partner_ptr;  /* host [nz+1]: via partners of each layer   */
+  const int32_t* partner_z;    /* host, ascending within each layer         */
+  const float* partner_cost;   /* host, float32 via cost of that pair       */
+  const int32_t* partner_site; /* host, 0 all, 1 checkerboard, k>=2 stride  */
+} ogr_lattice_desc;
+
+int ogr_csr_num_edges(const ogr_lattice_desc* d, int64_t* num_edges);
+size_t ogr_csr_workspace_bytes(const ogr_lattice_desc* d);
+/* Builds indptr[N+1], indices[E], base_costs[E], edge_layer[E], edge_kind[E],
+ * edge_src[E] and rev[E] (index of the opposite arc). */
+int ogr_csr_build(const ogr_lattice_desc* d, int32_t* indptr, int32_t* indices,
+                  float* base_costs, uint8_t* edge_layer, uint8_t* edge_kind,
+                  int32_t* edge_src, int32_t* rev, void* workspace,
+                  size_t workspace_bytes, void* stream);
+
+/* --------------------------------------------------------------- A2–A4 ---
+ * EdgeAccountant.update_costs (unified_pathfinder.py:1301-1384):
+ *   total = base*vmult*bw*bias + (pres*bias)*max(0,ema-cap) + hw*history,
+ *   +inf on blocked arcs, + float32(e) % 9973 * 1e-6.
+ * layer_bias may be NULL (no per-layer bias).  blocked may be NULL.
+ */
+typedef struct {
+  int64_t num_edges;
+  const float* base_costs;
+  const uint8_t* edge_layer;
+  const uint8_t* edge_kind;
+  const float* present_ema;
+  const float* capacity;
+  const float* history;
+  const uint8_t* blocked;
+  const float* layer_bias;     /* device [nz] float32 or NULL */
+  float via_cost_multiplier;
+  float base_cost_weight;
+  float pres_fac;
+  float hist_weight;
+  int32_t add_jitter;
+} ogr_cost_args;
+
+int ogr_costs_update(const ogr_cost_args* a, float* total_cost, void* stream);
+
+/* begin_live_present_costs (unified_pathfinder.py:1386-1401):
+ * live_static = total - scale*max(0,ema-cap); total = live_static +
+ * scale*max(0,present+1-cap); scale = pres_fac*bias (vias: pres_fac). */
+int ogr_live_begin(const ogr_cost_args* a, const float* present, float* total_cost,
+                   float* live_static, void* stream);
+
+/* update_present_ema (unified_pathfinder.py:1291-1299). */
+int ogr_present_ema(int64_t num_edges, const float* present, float* present_ema,
+                    float beta, float one_minus_beta, void* stream);
+
+/* update_history (unified_pathfinder.py:1226-1289) with the loop's raw-present
+ * and 15x base-cost cap settings passed in. base_costs NULL = no cap. */
+int ogr_history_update(int64_t num_edges, float* history, const float* present,
+                       const float* present_ema, const float* capacity,
+                       const float* base_costs, float gain, float cap_mult,
+                       float decay, int32_t use_raw_present, void* stream);
+
+/* ------------------------------------------------------------------ A9 ---
+ * Tallies (compute_overuse :1137-1190, _compute_path_node_overuse
+ * :10718-10726, _compute_layer_bias's bincount :8473-8500).
+ * out[0] = Σ max(0,present-cap) over canonical arcs (src<dst) or all arcs,
+ * out[1] = number of such arcs > 0, out[2] = Σ max(0,use-1) over nodes,
+ * out[3] = nodes with use > 1; layer_units[z] = Σ over arcs of layer z of
+ * max(0,ema-cap) in units of 2^-23 plus Σ max(0,use-1) of layer z in units
+ * of 2^-23 (exact integers; the host divides).  out[4] != 0 flags an EMA
+ * value off the 2^-23 grid.  out (int64[5]) and layer_units (int64[nz]) are
+ * device arrays, zeroed here. */
+int ogr_tally(int64_t num_edges, int32_t num_nodes, int32_t nz, const float* present,
+              const float* present_ema, const float* capacity, const int32_t* edge_src,
+              const int32_t* indices, const uint8_t* edge_layer, const int32_t* path_node_use,
+              int32_t canonical_only, int64_t* out, int64_t* layer_units, void* stream);
+
+/* ------------------------------------------------------------- A6–A8 ---
+ * Route one net: rip-up of its old path (optional), bidirectional BFS ROI
+ * (extract_roi_bfs :2257-2384), exact ROI SSSP (find_path_roi :2451-2548),
+ * backtrace, and commit (commit_path :1096, refresh_live_present_costs
+ * :1403, _mark_path_node_use :4635, _mark_via_barrel_ownership_for_path
+ * :4934, _path_to_edges :9981-10046).
+ */
+typedef struct {
+  int32_t nx, ny, nz;
+  int32_t num_nodes;
+  int64_t num_edges;
+  const int32_t* indptr;
+  const int32_t* indices;
+  const int32_t* rev;
+  const uint8_t* blocked;      /* NULL: none */
+} ogr_graph;
+
+typedef struct {
+  float* total_cost;           /* live total cost (read by the search)       */
+  const float* live_static;    /* static part for live-present refresh        */
+  float* present;
+  const float* capacity;
+  const float* layer_bias;     /* device [nz] float32 of the cost update, or NULL */
+  const uint8_t* edge_layer;
+  const uint8_t* edge_kind;
+  int32_t* path_node_use;
+  int32_t* owner_count;        /* barrel ownership: #nets per node            */
+  int32_t* owner_xor;          /* XOR of those net ids (= id when count==1)   */
+  const float* node_history;
+} ogr_state;
+
+typedef struct {
+  int32_t net_id;
+  int32_t src, dst;
+  int32_t full_graph;          /* 1: ROI = whole graph (Manhattan >= 125)     */
+  int32_t bfs_max_depth;       /* min(int(radius + 2*bonus), 80)              */
+  int32_t bfs_halo;            /* min(16, 2 + int(max(0,bonus)/0.6))          */
+  double bfs_stop_count;       /* early stop when seen > this (1.5*max nodes) */
+  int32_t max_roi_nodes;       /* 50,000 in the reference                     */
+  float owner_weight;          /* float32(25*pres_fac) (or the cleanup value) */
+  float path_weight;           /* float32(25*pres_fac)                        */
+  float history_weight;        /* float32(5.0)                                */
+  int32_t penalty_enabled;     /* 0: no node penalty at all                   */
+} ogr_net_args;
+
+/* Per-search scratch (one "slot"): about 70 bytes per lattice node.  It must
+ * be initialised once with ogr_route_workspace_init; every search leaves it
+ * initialised again.  Two searches must not share a slot concurrently. */
+size_t ogr_route_workspace_bytes(int32_t num_nodes);
+int ogr_route_workspace_init(void* workspace, size_t workspace_bytes, int32_t num_nodes,
+                             void* stream);
+
+/* Search only (no state change).  path_out: device int32[path_cap];
+ * *path_len_out (host) = nodes written.  stats (device int64[4], may be
+ * NULL): arcs the sequential heap search scans before it pops dst, nodes it
+ * pops, ROI size, settle phases.  Returns OGR_OK / OGR_NO_PATH / an error;
+ * synchronises the stream to read the status. */
+int ogr_find_path(const ogr_graph* g, const ogr_state* st, const ogr_net_args* net,
+                  void* workspace, size_t workspace_bytes, int32_t* path_out,
+                  int32_t path_cap, int32_t* path_len_out, int64_t* stats, void* stream);
+
+/* Commit (sign=+1) or rip up (sign=-1) a path given as device node ids:
+ * present +-1 (floored at 0), live-present refresh of those arcs when
+ * live != 0, path-node use +-1, barrel ownership of every node spanned by a
+ * via hop.  Writes the arc list (forward then reverse, like _path_to_edges)
+ * into arcs_out[2*(len-1)] when not NULL, and OGR_OK / OGR_ERR_ARG (a hop is
+ * not an arc) into the device word *status_dev.  Asynchronous. */
+int ogr_path_apply(const ogr_graph* g, const ogr_state* st, const int32_t* path, int32_t len,
+                   int32_t net_id, int32_t sign, float pres_fac_f32, int32_t live,
+                   int32_t* arcs_out, int32_t* status_dev, void* stream);
+
+/* ROI only (for tests / scheduling): writes the ROI node list in the
+ * reference's order and its size.  Synchronises. */
+int ogr_extract_roi(const ogr_graph* g, const ogr_net_args* net, void* workspace,
+                    size_t workspace_bytes, int32_t* roi_out, int32_t roi_cap,
+                    int32_t* roi_len_out, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ORTHOROUTE_GB300_H */

@@ -1,0 +1,108 @@
+"""ctypes binding of ``include/orthoroute_gb300.h``.
+
+The library is built in-tree by ``orthoroute_gb300._build``.  There is no CPU
+fallback: if the shared library is missing or a CUDA device is absent, the
+routing entry points raise.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+from . import _build
+
+OGR_OK = 0
+OGR_NO_PATH = 1
+ERRORS = {-1: "bad argument", -2: "CUDA error", -3: "buffer capacity exceeded",
+          -4: "device loop iteration limit reached", -5: "exactness precondition violated"}
+
+EXPORTED = [
+    "ogr_csr_num_edges", "ogr_csr_workspace_bytes", "ogr_csr_build",
+    "ogr_costs_update", "ogr_live_begin", "ogr_present_ema", "ogr_history_update",
+    "ogr_tally", "ogr_route_workspace_bytes", "ogr_route_workspace_init",
+    "ogr_find_path", "ogr_path_apply", "ogr_extract_roi",
+]
+
+P = C.c_void_p
+I32 = C.c_int32
+I64 = C.c_int64
+F32 = C.c_float
+
+
+class LatticeDesc(C.Structure):
+    _fields_ = [("nx", I32), ("ny", I32), ("nz", I32), ("lateral_cost", F32), ("wrong_way_cost", F32),
+                ("layer_axis", P), ("partner_ptr", P), ("partner_z", P), ("partner_cost", P),
+                ("partner_site", P)]
+
+
+class CostArgs(C.Structure):
+    _fields_ = [("num_edges", I64), ("base_costs", P), ("edge_layer", P), ("edge_kind", P),
+                ("present_ema", P), ("capacity", P), ("history", P), ("blocked", P), ("layer_bias", P),
+                ("via_cost_multiplier", F32), ("base_cost_weight", F32), ("pres_fac", F32),
+                ("hist_weight", F32), ("add_jitter", I32)]
+
+
+class Graph(C.Structure):
+    _fields_ = [("nx", I32), ("ny", I32), ("nz", I32), ("num_nodes", I32), ("num_edges", I64),
+                ("indptr", P), ("indices", P), ("rev", P), ("blocked", P)]
+
+
+class State(C.Structure):
+    _fields_ = [("total_cost", P), ("live_static", P), ("present", P), ("capacity", P), ("layer_bias", P),
+                ("edge_layer", P), ("edge_kind", P), ("path_node_use", P), ("owner_count", P),
+                ("owner_xor", P), ("node_history", P)]
+
+
+class NetArgs(C.Structure):
+    _fields_ = [("net_id", I32), ("src", I32), ("dst", I32), ("full_graph", I32), ("bfs_max_depth", I32),
+                ("bfs_halo", I32), ("bfs_stop_count", C.c_double), ("max_roi_nodes", I32),
+                ("owner_weight", F32), ("path_weight", F32), ("history_weight", F32),
+                ("penalty_enabled", I32)]
+
+
+_LIB = None
+
+
+def lib_path() -> str:
+    return _build.LIB
+
+
+def load(build_if_missing: bool = True):
+    """Load the shared library (building it first if it is absent)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = _build.LIB
+    if not os.path.exists(path):
+        if not build_if_missing:
+            raise RuntimeError(f"{path} is missing; run orthoroute_gb300._build.build()")
+        _build.build()
+    lib = C.CDLL(path)
+    sig = {
+        "ogr_csr_num_edges": [C.POINTER(LatticeDesc), C.POINTER(I64)],
+        "ogr_csr_workspace_bytes": [C.POINTER(LatticeDesc)],
+        "ogr_csr_build": [C.POINTER(LatticeDesc), P, P, P, P, P, P, P, P, C.c_size_t, P],
+        "ogr_costs_update": [C.POINTER(CostArgs), P, P],
+        "ogr_live_begin": [C.POINTER(CostArgs), P, P, P, P],
+        "ogr_present_ema": [I64, P, P, F32, F32, P],
+        "ogr_history_update": [I64, P, P, P, P, P, F32, F32, F32, I32, P],
+        "ogr_tally": [I64, I32, I32, P, P, P, P, P, P, P, I32, P, P, P],
+        "ogr_route_workspace_bytes": [I32],
+        "ogr_route_workspace_init": [P, C.c_size_t, I32, P],
+        "ogr_find_path": [C.POINTER(Graph), C.POINTER(State), C.POINTER(NetArgs), P, C.c_size_t, P, I32,
+                          C.POINTER(I32), P, P],
+        "ogr_path_apply": [C.POINTER(Graph), C.POINTER(State), P, I32, I32, I32, F32, I32, P, P, P],
+        "ogr_extract_roi": [C.POINTER(Graph), C.POINTER(NetArgs), P, C.c_size_t, P, I32, C.POINTER(I32), P],
+    }
+    for name, args in sig.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = C.c_size_t if name.endswith("_bytes") else C.c_int
+    _LIB = lib
+    return lib
+
+
+def check(rc: int, what: str) -> int:
+    if rc < 0:
+        raise RuntimeError(f"{what} failed: {ERRORS.get(rc, rc)} ({rc})")
+    return rc

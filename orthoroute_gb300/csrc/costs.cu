@@ -1,0 +1,180 @@
+// A2–A4: per-arc cost update, live-present rebase, present EMA, history;
+// A9: overuse / node-use / per-layer tallies.
+//
+// All arithmetic is float32 with one rounding per operation in the order
+// numpy evaluates the reference's expressions (explicit __f*_rn intrinsics,
+// so no FMA contraction can merge two roundings).  These kernels stream
+// 6–8 arrays of E entries once: HBM-bound, grid-stride over 152 SMs.
+#include "common.cuh"
+
+namespace {
+
+constexpr int kThreads = 256;
+
+__device__ __forceinline__ float arc_bias(const float* layer_bias, unsigned char layer, unsigned char kind) {
+  return (layer_bias != nullptr && kind == 0) ? layer_bias[layer] : 1.0f;
+}
+
+// float32(e) % 9973 * float32(1e-6): numpy's arange(E, float32) rounds e to
+// nearest even like __int2float_rn; fmodf is exact.
+__device__ __forceinline__ float jitter(int64_t e) {
+  const float fe = __ll2float_rn((long long)e);
+  return __fmul_rn(fmodf(fe, 9973.0f), 1e-6f);
+}
+
+__global__ void cost_kernel(ogr_cost_args a, float* __restrict__ total) {
+  const bool have_bias = a.layer_bias != nullptr;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < a.num_edges;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const unsigned char lay = a.edge_layer[e], kind = a.edge_kind[e];
+    const float over = fmaxf(0.0f, __fsub_rn(a.present_ema[e], a.capacity[e]));
+    const float bias = arc_bias(a.layer_bias, lay, kind);
+    // adjusted = ((base * vmult) * bw) * bias
+    float adj = __fmul_rn(__fmul_rn(a.base_costs[e], a.via_cost_multiplier), a.base_cost_weight);
+    if (have_bias) adj = __fmul_rn(adj, bias);
+    // present = (pres_fac * bias) * over
+    const float scale = have_bias ? __fmul_rn(a.pres_fac, bias) : a.pres_fac;
+    const float pres = __fmul_rn(scale, over);
+    float t = __fadd_rn(__fadd_rn(adj, pres), __fmul_rn(a.hist_weight, a.history[e]));
+    if (a.blocked != nullptr && a.blocked[e]) t = __int_as_float(0x7f800000);
+    if (a.add_jitter) t = __fadd_rn(t, jitter(e));
+    total[e] = t;
+  }
+}
+
+__global__ void live_kernel(ogr_cost_args a, const float* __restrict__ present, float* __restrict__ total,
+                            float* __restrict__ live_static) {
+  const bool have_bias = a.layer_bias != nullptr;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < a.num_edges;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const float bias = arc_bias(a.layer_bias, a.edge_layer[e], a.edge_kind[e]);
+    const float scale = have_bias ? __fmul_rn(a.pres_fac, bias) : a.pres_fac;
+    const float cap = a.capacity[e];
+    const float it_over = fmaxf(0.0f, __fsub_rn(a.present_ema[e], cap));
+    const float st = __fsub_rn(total[e], __fmul_rn(scale, it_over));
+    const float prosp = fmaxf(0.0f, __fsub_rn(__fadd_rn(present[e], 1.0f), cap));
+    live_static[e] = st;
+    total[e] = __fadd_rn(st, __fmul_rn(scale, prosp));
+  }
+}
+
+__global__ void ema_kernel(int64_t E, const float* __restrict__ present, float* __restrict__ ema, float beta,
+                           float omb) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < E; e += (int64_t)gridDim.x * blockDim.x)
+    ema[e] = __fadd_rn(__fmul_rn(beta, present[e]), __fmul_rn(omb, ema[e]));
+}
+
+__global__ void history_kernel(int64_t E, float* __restrict__ hist, const float* __restrict__ src,
+                               const float* __restrict__ cap, const float* __restrict__ base, float gain,
+                               float cap_mult, float decay) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < E; e += (int64_t)gridDim.x * blockDim.x) {
+    float h = __fmul_rn(hist[e], decay);
+    const float over = fmaxf(0.0f, __fsub_rn(src[e], cap[e]));
+    float inc = __fmul_rn(gain, over);
+    if (base != nullptr) inc = fminf(inc, __fmul_rn(cap_mult, base[e]));
+    hist[e] = __fadd_rn(h, inc);
+  }
+}
+
+// Exact integer tallies.  Per-layer EMA overuse is accumulated in units of
+// 2^-23 (every max(0, ema-1) with ema >= 1 is a multiple of 2^-23, so the
+// sum is exact and order independent, like numpy's float64 bincount).
+constexpr int kMaxLayers = 64;
+
+__global__ void tally_kernel(int64_t E, int32_t N, int32_t nz, const float* __restrict__ present,
+                             const float* __restrict__ ema, const float* __restrict__ cap,
+                             const int32_t* __restrict__ edge_src, const int32_t* __restrict__ indices,
+                             const unsigned char* __restrict__ edge_layer, const int32_t* __restrict__ use,
+                             int canonical_only, unsigned long long* out, unsigned long long* layer_units) {
+  __shared__ unsigned long long s_layer[kMaxLayers];
+  __shared__ unsigned long long s_out[5];
+  for (int i = threadIdx.x; i < nz; i += blockDim.x) s_layer[i] = 0;
+  if (threadIdx.x < 5) s_out[threadIdx.x] = 0;
+  __syncthreads();
+  unsigned long long over_sum = 0, over_cnt = 0, bad = 0;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < E; e += (int64_t)gridDim.x * blockDim.x) {
+    const float c = cap[e];
+    if (!canonical_only || edge_src[e] < indices[e]) {
+      const float o = fmaxf(0.0f, __fsub_rn(present[e], c));
+      if (o > 0.0f) {
+        over_sum += (unsigned long long)o;
+        over_cnt += 1;
+      }
+    }
+    const float eo = fmaxf(0.0f, __fsub_rn(ema[e], c));
+    if (eo > 0.0f) {
+      const double units = (double)eo * 8388608.0;  // 2^23
+      const unsigned long long u = (unsigned long long)units;
+      if ((double)u != units) bad = 1;
+      atomicAdd(&s_layer[edge_layer[e]], u);
+    }
+  }
+  const int64_t plane = (int64_t)N / nz;
+  unsigned long long nsum = 0, ncnt = 0;
+  for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < N; n += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t u = use[n];
+    if (u > 1) {
+      nsum += (unsigned long long)(u - 1);
+      ncnt += 1;
+      atomicAdd(&s_layer[(int)(n / plane)], (unsigned long long)(u - 1) << 23);
+    }
+  }
+  atomicAdd(&s_out[0], over_sum);
+  atomicAdd(&s_out[1], over_cnt);
+  atomicAdd(&s_out[2], nsum);
+  atomicAdd(&s_out[3], ncnt);
+  if (bad) atomicOr(&s_out[4], 1ull);
+  __syncthreads();
+  if (threadIdx.x < 5) atomicAdd(&out[threadIdx.x], s_out[threadIdx.x]);
+  for (int i = threadIdx.x; i < nz; i += blockDim.x) atomicAdd(&layer_units[i], s_layer[i]);
+}
+
+}  // namespace
+
+extern "C" int ogr_costs_update(const ogr_cost_args* a, float* total_cost, void* stream) {
+  if (!a || !total_cost || a->num_edges < 0) return OGR_ERR_ARG;
+  cost_kernel<<<ogr_blocks(a->num_edges, kThreads, 152 * 32), kThreads, 0, ogr_stream(stream)>>>(*a, total_cost);
+  OGR_LAUNCH_CHECK();
+  return OGR_OK;
+}
+
+extern "C" int ogr_live_begin(const ogr_cost_args* a, const float* present, float* total_cost, float* live_static,
+                              void* stream) {
+  if (!a || !present || !total_cost || !live_static) return OGR_ERR_ARG;
+  live_kernel<<<ogr_blocks(a->num_edges, kThreads, 152 * 32), kThreads, 0, ogr_stream(stream)>>>(
+      *a, present, total_cost, live_static);
+  OGR_LAUNCH_CHECK();
+  return OGR_OK;
+}
+
+extern "C" int ogr_present_ema(int64_t E, const float* present, float* ema, float beta, float omb, void* stream) {
+  if (!present || !ema) return OGR_ERR_ARG;
+  ema_kernel<<<ogr_blocks(E, kThreads, 152 * 32), kThreads, 0, ogr_stream(stream)>>>(E, present, ema, beta, omb);
+  OGR_LAUNCH_CHECK();
+  return OGR_OK;
+}
+
+extern "C" int ogr_history_update(int64_t E, float* history, const float* present, const float* present_ema,
+                                  const float* capacity, const float* base_costs, float gain, float cap_mult,
+                                  float decay, int32_t use_raw_present, void* stream) {
+  if (!history || !present || !present_ema || !capacity) return OGR_ERR_ARG;
+  history_kernel<<<ogr_blocks(E, kThreads, 152 * 32), kThreads, 0, ogr_stream(stream)>>>(
+      E, history, use_raw_present ? present : present_ema, capacity, base_costs, gain, cap_mult, decay);
+  OGR_LAUNCH_CHECK();
+  return OGR_OK;
+}
+
+extern "C" int ogr_tally(int64_t E, int32_t N, int32_t nz, const float* present, const float* present_ema,
+                         const float* capacity, const int32_t* edge_src, const int32_t* indices,
+                         const uint8_t* edge_layer, const int32_t* path_node_use, int32_t canonical_only,
+                         int64_t* out, int64_t* layer_units, void* stream) {
+  if (nz < 1 || nz > kMaxLayers || N % nz != 0) return OGR_ERR_ARG;
+  cudaStream_t s = ogr_stream(stream);
+  OGR_CUDA_TRY(cudaMemsetAsync(out, 0, 5 * sizeof(int64_t), s));
+  OGR_CUDA_TRY(cudaMemsetAsync(layer_units, 0, nz * sizeof(int64_t), s));
+  tally_kernel<<<ogr_blocks(E, kThreads, 152 * 8), kThreads, 0, s>>>(
+      E, N, nz, present, present_ema, capacity, edge_src, indices, edge_layer, path_node_use, canonical_only,
+      reinterpret_cast<unsigned long long*>(out), reinterpret_cast<unsigned long long*>(layer_units));
+  OGR_LAUNCH_CHECK();
+  return OGR_OK;
+}

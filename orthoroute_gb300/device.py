@@ -1,0 +1,216 @@
+"""Device-resident lattice and congestion state, and thin wrappers over the C ABI.
+
+PyTorch tensors provide the device memory; every computation on them is a
+hand-written kernel in ``csrc/``.  Arrays (E arcs, N nodes):
+
+* CSR: indptr int32[N+1], indices int32[E], base_costs f32[E],
+  edge_layer u8[E], edge_kind u8[E], edge_src int32[E], rev int32[E]
+* accounting: present, present_ema, history, capacity, total_cost,
+  live_static f32[E]; layer_bias f32[Nz]
+* nodes: path_node_use, owner_count, owner_xor int32[N], node_history f32[N]
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import List, Optional, Sequence
+
+import numpy as np
+import torch
+
+from . import _lib
+from .lattice import Lattice
+
+
+def _p(t: Optional[torch.Tensor]) -> Optional[int]:
+    return None if t is None else t.data_ptr()
+
+
+def _stream_ptr(stream: Optional[torch.cuda.Stream]) -> Optional[int]:
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return s.cuda_stream
+
+
+def require_cuda():
+    if not torch.cuda.is_available():
+        raise RuntimeError("orthoroute_gb300 needs a CUDA device (GB300, sm_103a); there is no CPU path")
+
+
+class DeviceGraph:
+    """CSR lattice built on the device by ``ogr_csr_build``."""
+
+    def __init__(self, lattice: Lattice, device="cuda", stream=None):
+        require_cuda()
+        self.lib = _lib.load()
+        self.lattice = lattice
+        self.device = torch.device(device)
+        desc, keep = lattice.descriptor()
+        E = C.c_int64(0)
+        _lib.check(self.lib.ogr_csr_num_edges(C.byref(desc), C.byref(E)), "ogr_csr_num_edges")
+        self.E = int(E.value)
+        self.N = lattice.num_nodes
+        dev = self.device
+        self.indptr = torch.empty(self.N + 1, dtype=torch.int32, device=dev)
+        self.indices = torch.empty(self.E, dtype=torch.int32, device=dev)
+        self.base_costs = torch.empty(self.E, dtype=torch.float32, device=dev)
+        self.edge_layer = torch.empty(self.E, dtype=torch.uint8, device=dev)
+        self.edge_kind = torch.empty(self.E, dtype=torch.uint8, device=dev)
+        self.edge_src = torch.empty(self.E, dtype=torch.int32, device=dev)
+        self.rev = torch.empty(self.E, dtype=torch.int32, device=dev)
+        ws_bytes = int(self.lib.ogr_csr_workspace_bytes(C.byref(desc)))
+        ws = torch.empty(ws_bytes, dtype=torch.uint8, device=dev)
+        _lib.check(self.lib.ogr_csr_build(C.byref(desc), _p(self.indptr), _p(self.indices), _p(self.base_costs),
+                                          _p(self.edge_layer), _p(self.edge_kind), _p(self.edge_src),
+                                          _p(self.rev), _p(ws), ws_bytes, _stream_ptr(stream)),
+                   "ogr_csr_build")
+        self.blocked = None
+        del keep
+
+    def cgraph(self) -> _lib.Graph:
+        L = self.lattice
+        return _lib.Graph(L.nx, L.ny, L.nz, self.N, self.E, _p(self.indptr), _p(self.indices), _p(self.rev),
+                          _p(self.blocked))
+
+
+class DeviceState:
+    """Congestion state of one routing job (EdgeAccountant + node maps)."""
+
+    def __init__(self, graph: DeviceGraph):
+        self.g = graph
+        dev, E, N = graph.device, graph.E, graph.N
+        self.present = torch.zeros(E, dtype=torch.float32, device=dev)
+        self.present_ema = torch.zeros(E, dtype=torch.float32, device=dev)
+        self.history = torch.zeros(E, dtype=torch.float32, device=dev)
+        self.capacity = torch.ones(E, dtype=torch.float32, device=dev)
+        self.total_cost = torch.zeros(E, dtype=torch.float32, device=dev)
+        self.live_static = torch.zeros(E, dtype=torch.float32, device=dev)
+        self.layer_bias = torch.ones(graph.lattice.nz, dtype=torch.float32, device=dev)
+        self.use_layer_bias = False
+        self.path_node_use = torch.zeros(N, dtype=torch.int32, device=dev)
+        self.owner_count = torch.zeros(N, dtype=torch.int32, device=dev)
+        self.owner_xor = torch.zeros(N, dtype=torch.int32, device=dev)
+        self.node_history = torch.zeros(N, dtype=torch.float32, device=dev)
+
+    def cstate(self) -> _lib.State:
+        g = self.g
+        return _lib.State(_p(self.total_cost), _p(self.live_static), _p(self.present), _p(self.capacity),
+                          _p(self.layer_bias) if self.use_layer_bias else None, _p(g.edge_layer), _p(g.edge_kind),
+                          _p(self.path_node_use), _p(self.owner_count), _p(self.owner_xor), _p(self.node_history))
+
+    def cost_args(self, pres_fac, hist_weight, via_mult, base_weight, add_jitter=True) -> _lib.CostArgs:
+        g = self.g
+        return _lib.CostArgs(g.E, _p(g.base_costs), _p(g.edge_layer), _p(g.edge_kind), _p(self.present_ema),
+                             _p(self.capacity), _p(self.history), _p(g.blocked),
+                             _p(self.layer_bias) if self.use_layer_bias else None,
+                             float(np.float32(via_mult)), float(np.float32(base_weight)),
+                             float(np.float32(pres_fac)), float(np.float32(hist_weight)), int(bool(add_jitter)))
+
+
+class Ops:
+    """Typed wrappers over the kernels for one graph / state pair."""
+
+    def __init__(self, graph: DeviceGraph, state: DeviceState, slots: int = 1, stream=None):
+        self.g, self.s = graph, state
+        self.lib = graph.lib
+        self.stream = stream
+        self.ws_bytes = int(self.lib.ogr_route_workspace_bytes(graph.N))
+        self.ws = [torch.empty(self.ws_bytes, dtype=torch.uint8, device=graph.device) for _ in range(slots)]
+        for w in self.ws:
+            _lib.check(self.lib.ogr_route_workspace_init(_p(w), self.ws_bytes, graph.N, self._sp()),
+                       "ogr_route_workspace_init")
+        self.path_buf = torch.empty(max(graph.N, 2), dtype=torch.int32, device=graph.device)
+        self.stats = torch.zeros(4, dtype=torch.int64, device=graph.device)
+        self.status = torch.zeros(1, dtype=torch.int32, device=graph.device)
+        self.tally_out = torch.zeros(5, dtype=torch.int64, device=graph.device)
+        self.layer_units = torch.zeros(graph.lattice.nz, dtype=torch.int64, device=graph.device)
+
+    def _sp(self):
+        return _stream_ptr(self.stream)
+
+    # -- A2–A4 ----------------------------------------------------------------
+    def update_costs(self, pres_fac, hist_weight, via_mult, base_weight, layer_bias: Optional[np.ndarray]):
+        s = self.s
+        s.use_layer_bias = layer_bias is not None
+        if layer_bias is not None:
+            s.layer_bias.copy_(torch.from_numpy(np.asarray(layer_bias, dtype=np.float32)))
+        a = s.cost_args(pres_fac, hist_weight, via_mult, base_weight)
+        _lib.check(self.lib.ogr_costs_update(C.byref(a), _p(s.total_cost), self._sp()), "ogr_costs_update")
+
+    def live_begin(self, pres_fac):
+        s = self.s
+        a = s.cost_args(pres_fac, 0.0, 1.0, 1.0)
+        _lib.check(self.lib.ogr_live_begin(C.byref(a), _p(s.present), _p(s.total_cost), _p(s.live_static),
+                                           self._sp()), "ogr_live_begin")
+
+    def present_ema(self, beta=0.40):
+        s = self.s
+        _lib.check(self.lib.ogr_present_ema(self.g.E, _p(s.present), _p(s.present_ema), float(np.float32(beta)),
+                                            float(np.float32(1.0 - beta)), self._sp()), "ogr_present_ema")
+
+    def update_history(self, gain, cap_mult=15.0, decay=1.0, use_cap=True, use_raw_present=True):
+        s = self.s
+        _lib.check(self.lib.ogr_history_update(self.g.E, _p(s.history), _p(s.present), _p(s.present_ema),
+                                               _p(s.capacity), _p(self.g.base_costs) if use_cap else None,
+                                               float(np.float32(gain)), float(np.float32(cap_mult)),
+                                               float(np.float32(decay)), int(use_raw_present), self._sp()),
+                   "ogr_history_update")
+
+    def tally(self, canonical_only=True):
+        """Returns (over_sum, over_cnt, node_over_sum, node_over_cnt, layer_units[nz])."""
+        s, g = self.s, self.g
+        _lib.check(self.lib.ogr_tally(g.E, g.N, g.lattice.nz, _p(s.present), _p(s.present_ema), _p(s.capacity),
+                                      _p(g.edge_src), _p(g.indices), _p(g.edge_layer), _p(s.path_node_use),
+                                      int(canonical_only), _p(self.tally_out), _p(self.layer_units), self._sp()),
+                   "ogr_tally")
+        out = self.tally_out.cpu().numpy()
+        if out[4]:
+            raise RuntimeError("present EMA off the 2^-23 grid: per-layer sums would not be exact")
+        return int(out[0]), int(out[1]), int(out[2]), int(out[3]), self.layer_units.cpu().numpy()
+
+    # -- A6–A8 ----------------------------------------------------------------
+    def net_args(self, net_id, src, dst, *, full_graph=False, max_depth=80, halo=2, max_roi_nodes=50_000,
+                 pres_fac=1.0, owner_base=25.0, path_base=25.0, hist_pen=5.0, freeze_weight=None,
+                 penalty=True) -> _lib.NetArgs:
+        w = float(owner_base) * float(pres_fac)
+        if freeze_weight is not None:
+            w = max(w, float(freeze_weight))
+        return _lib.NetArgs(int(net_id), int(src), int(dst), int(bool(full_graph)), int(max_depth), int(halo),
+                            float(max_roi_nodes) * 1.5, int(max_roi_nodes), float(np.float32(w)),
+                            float(np.float32(float(path_base) * float(pres_fac))), float(np.float32(hist_pen)),
+                            int(bool(penalty)))
+
+    def find_path(self, net: _lib.NetArgs, slot: int = 0) -> Optional[List[int]]:
+        g = self.g.cgraph()
+        st = self.s.cstate()
+        n = C.c_int32(0)
+        rc = self.lib.ogr_find_path(C.byref(g), C.byref(st), C.byref(net), _p(self.ws[slot]), self.ws_bytes,
+                                    _p(self.path_buf), int(self.path_buf.numel()), C.byref(n), _p(self.stats),
+                                    self._sp())
+        _lib.check(rc, "ogr_find_path")
+        if rc == _lib.OGR_NO_PATH or n.value < 2:
+            return None
+        return self.path_buf[: n.value].cpu().tolist()
+
+    def extract_roi(self, net: _lib.NetArgs, slot: int = 0) -> np.ndarray:
+        g = self.g.cgraph()
+        out = torch.empty(self.g.N, dtype=torch.int32, device=self.g.device)
+        n = C.c_int32(0)
+        _lib.check(self.lib.ogr_extract_roi(C.byref(g), C.byref(net), _p(self.ws[slot]), self.ws_bytes, _p(out),
+                                            self.g.N, C.byref(n), self._sp()), "ogr_extract_roi")
+        return out[: n.value].cpu().numpy()
+
+    def apply_path(self, path: Sequence[int], net_id: int, sign: int, pres_fac: float, live: bool = True):
+        """Commit (+1) or rip up (-1); returns the arc list (forward then reverse)."""
+        L = len(path)
+        if L < 2:
+            return []
+        d = torch.as_tensor(np.asarray(path, dtype=np.int32)).to(self.g.device)
+        arcs = torch.empty(2 * (L - 1), dtype=torch.int32, device=self.g.device)
+        g = self.g.cgraph()
+        st = self.s.cstate()
+        _lib.check(self.lib.ogr_path_apply(C.byref(g), C.byref(st), _p(d), L, int(net_id), int(sign),
+                                           float(np.float32(pres_fac)), int(bool(live)), _p(arcs),
+                                           _p(self.status), self._sp()), "ogr_path_apply")
+        out = arcs.cpu().tolist()
+        if int(self.status.item()) != 0:
+            raise ValueError("path hop is not a graph edge")
+        return out
