@@ -207,7 +207,7 @@ def detect_barrel_conflicts(edge_src, indices, node_state: NodeState, paths: Dic
         nid = net_id_map[name]
         res = net_to_edges.get(name)
         if res is None:
-            raise RuntimeError("edge tracking missing for committed net")
+            raise RuntimeError(f"edge tracking missing for committed net {name}")
         chunk = np.asarray(res, dtype=np.int32)[:len(res) // 2]
         if chunk.size == 0:
             continue
