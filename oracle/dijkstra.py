@@ -78,3 +78,49 @@ def find_path_roi(indptr, indices, src, dst, costs, roi_nodes, global_to_roi,
         cur = int(parent[cur])
     path.reverse()
     return path if len(path) > 1 else None
+
+
+# --- C restatement (same semantics, ~100x faster) ------------------------------
+_CLIB = None
+
+
+def _clib():
+    global _CLIB
+    if _CLIB is None:
+        import ctypes
+        from . import build as _b
+        lib = ctypes.CDLL(_b.build())
+        P = ctypes.c_void_p
+        lib.oracle_heap_dijkstra.argtypes = [ctypes.c_int32, ctypes.c_int32, P, P, P, P, ctypes.c_int32, P, P, P,
+                                             ctypes.POINTER(ctypes.c_int32), P]
+        lib.oracle_heap_dijkstra.restype = ctypes.c_int
+        _CLIB = lib
+    return _CLIB
+
+
+def find_path_roi_c(indptr, indices, src, dst, costs, roi_nodes, global_to_roi, node_penalty=None,
+                    stats=None) -> Optional[List[int]]:
+    """``find_path_roi`` through ``oracle/csrc/heap_dijkstra.c``."""
+    import ctypes
+    lib = _clib()
+    ip = np.ascontiguousarray(indptr, dtype=np.int32)
+    ix = np.ascontiguousarray(indices, dtype=np.int32)
+    c = np.ascontiguousarray(costs, dtype=np.float32)
+    roi = np.ascontiguousarray(roi_nodes, dtype=np.int32)
+    g2r = np.ascontiguousarray(global_to_roi, dtype=np.int32)
+    pen = None if node_penalty is None else np.ascontiguousarray(node_penalty, dtype=np.float32)
+    out = np.empty(max(len(roi), 2), dtype=np.int32)
+    n = ctypes.c_int32(0)
+    st = np.zeros(2, dtype=np.int64)
+    rc = lib.oracle_heap_dijkstra(int(src), int(dst), ip.ctypes.data, ix.ctypes.data, c.ctypes.data,
+                                  roi.ctypes.data, len(roi), g2r.ctypes.data,
+                                  None if pen is None else pen.ctypes.data, out.ctypes.data, ctypes.byref(n),
+                                  st.ctypes.data)
+    if rc < 0:
+        raise MemoryError("oracle heap Dijkstra allocation failed")
+    if stats is not None:
+        stats["scanned"] = stats.get("scanned", 0) + int(st[0])
+        stats["settled"] = stats.get("settled", 0) + int(st[1])
+    if rc != 0:
+        return None
+    return out[: n.value].tolist()

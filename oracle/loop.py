@@ -35,7 +35,7 @@ from typing import Dict, List, Optional, Set, Tuple
 import numpy as np
 
 from . import accounting as acc
-from .dijkstra import find_path_roi
+from .dijkstra import find_path_roi, find_path_roi_c
 from .lattice import LatticeSpec, build_csr
 from .roi import extract_roi_bfs, roi_radius
 from .tallies import NodeState, detect_barrel_conflicts, detect_path_node_conflicts, path_to_edges
@@ -269,8 +269,9 @@ def next_pressure_ceiling(cur, events, pressure_after=2, maximum=1024.0):
 class OracleRouter:
     """CPU restatement of the reference loop for (name, src, dst) tasks."""
 
-    def __init__(self, spec: LatticeSpec, bounds, cfg: Optional[Config] = None):
+    def __init__(self, spec: LatticeSpec, bounds, cfg: Optional[Config] = None, fast: bool = False):
         self.spec = spec
+        self._find = find_path_roi_c if fast else find_path_roi
         self.cfg = cfg or Config()
         self.csr = build_csr(spec)
         c = self.csr
@@ -598,8 +599,8 @@ class OracleRouter:
                                         self.cfg.node_history_penalty, freeze_weight=freeze)
 
     def _search(self, src, dst, roi, g2r, pen, name, kind):
-        path = find_path_roi(self.csr.indptr, self.csr.indices, src, dst, self.acc.total_cost, roi, g2r,
-                             node_penalty=pen, stats=self.stats)
+        path = self._find(self.csr.indptr, self.csr.indices, src, dst, self.acc.total_cost, roi, g2r,
+                          node_penalty=pen, stats=self.stats)
         self.stats["searches"] += 1
         if self.search_log is not None:
             self.search_log.append((self.iteration, name, kind, list(path) if path else None))

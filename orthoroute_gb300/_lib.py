@@ -20,7 +20,7 @@ EXPORTED = [
     "ogr_csr_num_edges", "ogr_csr_workspace_bytes", "ogr_csr_build",
     "ogr_costs_update", "ogr_live_begin", "ogr_present_ema", "ogr_history_update",
     "ogr_tally", "ogr_route_workspace_bytes", "ogr_route_workspace_init",
-    "ogr_find_path", "ogr_path_apply", "ogr_extract_roi",
+    "ogr_find_path", "ogr_path_apply", "ogr_extract_roi", "ogr_via_pools_apply", "ogr_overused_arcs",
 ]
 
 P = C.c_void_p
@@ -93,6 +93,8 @@ def load(build_if_missing: bool = True):
                           C.POINTER(I32), P, P],
         "ogr_path_apply": [C.POINTER(Graph), C.POINTER(State), P, I32, I32, I32, F32, I32, P, P, P],
         "ogr_extract_roi": [C.POINTER(Graph), C.POINTER(NetArgs), P, C.c_size_t, P, I32, C.POINTER(I32), P],
+        "ogr_via_pools_apply": [I64, I32, I32, I32, P, P, P, P, P, P, P, P, P, P, F32, F32, F32, I32, I32, P, P],
+        "ogr_overused_arcs": [I64, P, P, P, P, I32, P, P],
     }
     for name, args in sig.items():
         fn = getattr(lib, name)

@@ -178,3 +178,102 @@ extern "C" int ogr_tally(int64_t E, int32_t N, int32_t nz, const float* present,
   OGR_LAUNCH_CHECK();
   return OGR_OK;
 }
+
+// ---------------------------------------------------------------- A5 ---------
+// Via pool penalties (_apply_via_pooling_penalties CPU branch,
+// unified_pathfinder.py:5884-5980) and the hard block of saturated via
+// resources (_block_via_edges_with_collisions, :6094-6161), one thread per
+// via arc.  Pools are [Nx][Ny] / [Nx][Ny][segZ] (x-major, like the reference).
+// disc[z_lo*nz + z_hi] is the leave-hot-layer discount computed on the host
+// with the reference's dtypes; the penalty is rounded to float32 after the
+// product, which equals numpy's float32 multiply when the discount is float32.
+namespace {
+
+__global__ void via_pool_kernel(int64_t E, int32_t nx, int32_t ny, int32_t nz, const int32_t* __restrict__ edge_src,
+                                const int32_t* __restrict__ indices, const uint8_t* __restrict__ kind,
+                                const float* __restrict__ col_pres, const float* __restrict__ seg_prefix,
+                                const int16_t* __restrict__ col_use, const int16_t* __restrict__ col_cap,
+                                const int16_t* __restrict__ seg_use, const int8_t* __restrict__ seg_cap,
+                                const double* __restrict__ disc, float col_w, float seg_w, float pres_fac,
+                                int32_t apply_penalty, int32_t apply_block, float* __restrict__ total) {
+  const int64_t plane = (int64_t)nx * ny;
+  const int segZ = nz > 2 ? nz - 2 : 0;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < E; e += (int64_t)gridDim.x * blockDim.x) {
+    if (!kind[e]) continue;
+    const int32_t u = edge_src[e], v = indices[e];
+    const int zu = (int)(u / plane), zv = (int)(v / plane);
+    const int64_t r = u % plane;
+    const int y = (int)(r / nx), x = (int)(r % nx);
+    int zl = min(zu, zv), zh = max(zu, zv);
+    zl = min(max(zl, 1), nz - 2);
+    zh = min(max(zh, 1), nz - 2);
+    const int64_t cxy = (int64_t)x * ny + y;
+    if (apply_penalty) {
+      float pen = 0.0f;
+      pen = __fadd_rn(pen, __fmul_rn(col_w, col_pres[cxy]));
+      if (segZ > 0) {
+        const int hi = zh - 2, lo = zl - 2;
+        const float ph = (hi >= 0 && hi < segZ) ? seg_prefix[cxy * segZ + hi] : 0.0f;
+        const float pl = (lo >= 0 && lo < segZ) ? seg_prefix[cxy * segZ + lo] : 0.0f;
+        const float sp = (zh > zl) ? __fsub_rn(ph, pl) : __fmul_rn(__fsub_rn(ph, pl), 0.0f);
+        pen = __fadd_rn(pen, __fmul_rn(seg_w, sp));
+      }
+      if (disc != nullptr) pen = __double2float_rn((double)pen * disc[zl * nz + zh]);
+      if (pen > 0.0f) total[e] = __fadd_rn(total[e], __fmul_rn(pres_fac, pen));
+    }
+    if (apply_block) {
+      bool blocked = col_use[cxy] >= col_cap[cxy];
+      if (segZ > 0) {
+        for (int z = zl; z < zh && !blocked; ++z) {
+          const int s = z - 1;
+          if (s >= 0 && s < segZ && seg_use[cxy * segZ + s] >= seg_cap[cxy * segZ + s]) blocked = true;
+        }
+      }
+      if (blocked) total[e] = __int_as_float(0x7f800000);
+    }
+  }
+}
+
+__global__ void overused_kernel(int64_t E, const float* __restrict__ present, const float* __restrict__ cap,
+                                int32_t* __restrict__ out_idx, float* __restrict__ out_val, int32_t out_cap,
+                                unsigned int* __restrict__ count) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < E; e += (int64_t)gridDim.x * blockDim.x) {
+    const float o = fmaxf(0.0f, __fsub_rn(present[e], cap[e]));
+    if (o > 0.0f) {
+      const unsigned int p = atomicAdd(count, 1u);
+      if ((int32_t)p < out_cap) {
+        out_idx[p] = (int32_t)e;
+        out_val[p] = o;
+      }
+    }
+  }
+}
+
+}  // namespace
+
+extern "C" int ogr_via_pools_apply(int64_t E, int32_t nx, int32_t ny, int32_t nz, const int32_t* edge_src,
+                                   const int32_t* indices, const uint8_t* edge_kind, const float* col_pres,
+                                   const float* seg_prefix, const int16_t* col_use, const int16_t* col_cap,
+                                   const int16_t* seg_use, const int8_t* seg_cap, const double* discount,
+                                   float col_weight, float seg_weight, float pres_fac, int32_t apply_penalty,
+                                   int32_t apply_block, float* total_cost, void* stream) {
+  if (nz < 2 || !edge_src || !indices || !edge_kind || !total_cost) return OGR_ERR_ARG;
+  if (apply_penalty && !col_pres) return OGR_ERR_ARG;
+  if (apply_block && (!col_use || !col_cap)) return OGR_ERR_ARG;
+  via_pool_kernel<<<ogr_blocks(E, kThreads, 152 * 32), kThreads, 0, ogr_stream(stream)>>>(
+      E, nx, ny, nz, edge_src, indices, edge_kind, col_pres, seg_prefix, col_use, col_cap, seg_use, seg_cap, discount,
+      col_weight, seg_weight, pres_fac, apply_penalty, apply_block, total_cost);
+  OGR_LAUNCH_CHECK();
+  return OGR_OK;
+}
+
+extern "C" int ogr_overused_arcs(int64_t E, const float* present, const float* capacity, int32_t* out_idx,
+                                 float* out_val, int32_t out_cap, uint32_t* count, void* stream) {
+  if (!present || !capacity || !out_idx || !out_val || !count) return OGR_ERR_ARG;
+  cudaStream_t s = ogr_stream(stream);
+  OGR_CUDA_TRY(cudaMemsetAsync(count, 0, sizeof(uint32_t), s));
+  overused_kernel<<<ogr_blocks(E, kThreads, 152 * 32), kThreads, 0, s>>>(E, present, capacity, out_idx, out_val,
+                                                                          out_cap, count);
+  OGR_LAUNCH_CHECK();
+  return OGR_OK;
+}

@@ -122,6 +122,13 @@ class Ops:
         self.status = torch.zeros(1, dtype=torch.int32, device=graph.device)
         self.tally_out = torch.zeros(5, dtype=torch.int64, device=graph.device)
         self.layer_units = torch.zeros(graph.lattice.nz, dtype=torch.int64, device=graph.device)
+        self.counters = dict(launches=0, h2d_bytes=0, d2h_bytes=0, search_launches=0, search_ms=0.0)
+        self._ev0 = torch.cuda.Event(enable_timing=True)
+        self._ev1 = torch.cuda.Event(enable_timing=True)
+
+    def reset_counters(self):
+        for k in self.counters:
+            self.counters[k] = 0.0 if k == "search_ms" else 0
 
     def _sp(self):
         return _stream_ptr(self.stream)
@@ -134,17 +141,22 @@ class Ops:
             s.layer_bias.copy_(torch.from_numpy(np.asarray(layer_bias, dtype=np.float32)))
         a = s.cost_args(pres_fac, hist_weight, via_mult, base_weight)
         _lib.check(self.lib.ogr_costs_update(C.byref(a), _p(s.total_cost), self._sp()), "ogr_costs_update")
+        self.counters["launches"] += 1
+        if layer_bias is not None:
+            self.counters["h2d_bytes"] += 4 * len(layer_bias)
 
     def live_begin(self, pres_fac):
         s = self.s
         a = s.cost_args(pres_fac, 0.0, 1.0, 1.0)
         _lib.check(self.lib.ogr_live_begin(C.byref(a), _p(s.present), _p(s.total_cost), _p(s.live_static),
                                            self._sp()), "ogr_live_begin")
+        self.counters["launches"] += 1
 
     def present_ema(self, beta=0.40):
         s = self.s
         _lib.check(self.lib.ogr_present_ema(self.g.E, _p(s.present), _p(s.present_ema), float(np.float32(beta)),
                                             float(np.float32(1.0 - beta)), self._sp()), "ogr_present_ema")
+        self.counters["launches"] += 1
 
     def update_history(self, gain, cap_mult=15.0, decay=1.0, use_cap=True, use_raw_present=True):
         s = self.s
@@ -153,6 +165,7 @@ class Ops:
                                                float(np.float32(gain)), float(np.float32(cap_mult)),
                                                float(np.float32(decay)), int(use_raw_present), self._sp()),
                    "ogr_history_update")
+        self.counters["launches"] += 1
 
     def tally(self, canonical_only=True):
         """Returns (over_sum, over_cnt, node_over_sum, node_over_cnt, layer_units[nz])."""
@@ -162,6 +175,8 @@ class Ops:
                                       int(canonical_only), _p(self.tally_out), _p(self.layer_units), self._sp()),
                    "ogr_tally")
         out = self.tally_out.cpu().numpy()
+        self.counters["launches"] += 1
+        self.counters["d2h_bytes"] += 8 * (5 + g.lattice.nz)
         if out[4]:
             raise RuntimeError("present EMA off the 2^-23 grid: per-layer sums would not be exact")
         return int(out[0]), int(out[1]), int(out[2]), int(out[3]), self.layer_units.cpu().numpy()
@@ -182,10 +197,18 @@ class Ops:
         g = self.g.cgraph()
         st = self.s.cstate()
         n = C.c_int32(0)
+        stream = self.stream if self.stream is not None else torch.cuda.current_stream()
+        self._ev0.record(stream)
         rc = self.lib.ogr_find_path(C.byref(g), C.byref(st), C.byref(net), _p(self.ws[slot]), self.ws_bytes,
                                     _p(self.path_buf), int(self.path_buf.numel()), C.byref(n), _p(self.stats),
                                     self._sp())
+        self._ev1.record(stream)
         _lib.check(rc, "ogr_find_path")
+        self._ev1.synchronize()
+        self.counters["search_ms"] += self._ev0.elapsed_time(self._ev1)
+        self.counters["search_launches"] += 1
+        self.counters["launches"] += 1
+        self.counters["d2h_bytes"] += 16 + 4 * max(0, n.value)
         if rc == _lib.OGR_NO_PATH or n.value < 2:
             return None
         return self.path_buf[: n.value].cpu().tolist()
@@ -211,6 +234,9 @@ class Ops:
                                            float(np.float32(pres_fac)), int(bool(live)), _p(arcs),
                                            _p(self.status), self._sp()), "ogr_path_apply")
         out = arcs.cpu().tolist()
+        self.counters["launches"] += 1
+        self.counters["h2d_bytes"] += 4 * L
+        self.counters["d2h_bytes"] += 4 * (2 * (L - 1) + 1)
         if int(self.status.item()) != 0:
             raise ValueError("path hop is not a graph edge")
         return out

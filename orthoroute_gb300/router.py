@@ -1,0 +1,1380 @@
+"""``PathFinderRouter`` — the reference's router API over the GB300 kernels.
+
+Keeps the public surface of OrthoRoute's router
+(orthoroute/algorithms/manhattan/unified_pathfinder.py):
+
+* ``PathFinderRouter(config=None, use_gpu=None)``                 :2697
+* ``initialize_graph(board) -> bool``                             :2800
+* ``route_multiple_nets(requests, progress_cb=None, iteration_cb=None)``
+  with tuple requests ``(name, src, dst)`` or nets with ``.pads``  :4335
+* ``net_paths: Dict[str, List[int]]`` and the result dict keys   :7510-7534
+
+The negotiation policy (net order, hotsets, pressure schedule, cleanup
+gating, stagnation rip-up, best-state restore, detail pass) runs on the host
+exactly as the reference sequences it (:6163-7534); every step that touches
+per-arc or per-node arrays runs on the device: cost update, via-pool
+penalties and hard block, live-present rebase, ROI BFS + exact SSSP +
+backtrace per net, commit / rip-up scatter, history, present EMA and the
+overuse / layer tallies.  Host mirrors hold only what the policy reads at
+path granularity (node ownership members, path-node use, node history, via
+pools).  There is no CPU routing fallback: a missing CUDA device raises.
+"""
+from __future__ import annotations
+
+import heapq
+import math
+import os
+import random
+import time
+from collections import defaultdict
+from typing import Dict, List, Optional, Set, Tuple
+
+import numpy as np
+import torch
+
+from . import _lib
+from .device import DeviceGraph, DeviceState, Ops, require_cuda
+from .lattice import Lattice, default_layer_dirs
+
+ROI_THRESHOLD_STEPS = 125
+MAX_ROI_NODES = 50_000
+
+
+class PathFinderConfig:
+    """Router parameters (the fields of the reference's PathFinderConfig the
+    negotiation loop reads, with the same defaults, :570-782)."""
+
+    def __init__(self, **kw):
+        self.max_iterations = 40
+        self.owner_penalty_base = 25.0
+        self.path_node_penalty_base = 25.0
+        self.node_history_penalty = 5.0
+        self.node_history_increment = 1.0
+        self.pres_fac_init = 1.0
+        self.pres_fac_mult = 1.10
+        self.pres_fac_max = 64.0
+        self.hist_gain = 0.2
+        self.base_cost_weight = 0.3
+        self.grid_pitch = 0.4
+        self.preferred_layer_directions: Optional[List[str]] = None
+        self.wrong_way_cost_multiplier = float("inf")
+        self.via_cost = 0.7
+        self.via_pressure_threshold = 64
+        self.via_pressure_multiplier = 1.5
+        self.allow_any_layer_via: Optional[bool] = None
+        self.adjacent_via_step_scale = 4.0
+        self.via_diameter = 0.25
+        self.clearance = 0.15
+        self.via_drill = 0.15
+        self.min_hole_to_hole = 0.25
+        self.stagnation_patience = 5
+        self.slow_progress_window = 5
+        self.slow_progress_min_fraction = 0.025
+        self.slow_progress_min_overuse = 2048
+        self.slow_progress_hotset_cap = 512
+        self.slow_progress_hotset_growth_after = 2
+        self.slow_progress_hotset_cap_max = 1024
+        self.slow_progress_pressure_after = 2
+        self.slow_progress_pres_fac_max = 1024.0
+        self.slow_progress_pressure_trial_min_ratio = 0.80
+        self.slow_progress_pressure_trial_patience = 2
+        self.pressure_reference_hotset = 100
+        self.pressure_work_scale_max = 2.0
+        self.hist_cost_weight = 10.0
+        self.hotset_cap = 2048
+        self.hotset_cap_floor = 0
+        self.physical_hotset_cap = 1024
+        self.physical_hotset_min = 64
+        self.physical_conflicts_per_hotset_net = 50.0
+        self.via_keeper_rotation_overuse_threshold = 8
+        self.via_keeper_rotation_nets_per_step = 1024
+        self.portal_cleanup_edge_threshold = 3
+        self.portal_cleanup_node_penalty = 1_000_000.0
+        self.physical_cleanup_overuse_threshold = None
+        self.history_decay = None
+        self.live_present_costs = True
+        self.reroute_only_offenders = True
+        self.portal_enabled = False
+        self.use_gpu = True
+        self.layer_count = 6
+        self._explicit = set()
+        for k, v in kw.items():
+            setattr(self, k, v)
+
+    def __setattr__(self, k, v):
+        if k == "max_iterations" and hasattr(self, "_explicit"):
+            self._explicit.add(k)
+        object.__setattr__(self, k, v)
+
+
+# ------------------------------------------------------------- policy helpers
+def _history_hotset_cap(t):
+    if t <= 8:
+        return 16
+    if t <= 32:
+        return 32
+    if t <= 128:
+        return 64
+    if t <= 2048:
+        return 100
+    if t <= 16384:
+        return 180
+    return 256
+
+
+def _exploration_fraction(t):
+    return 0.15 if t > 16384 else 0.25 if t > 2048 else 0.40
+
+
+def _conflict_aware_hotset(ranked, pairs, cap, fraction, rng):
+    """Greedy pair cover + exploration (``_select_conflict_aware_hotset`` :8912-9037)."""
+    cap = max(0, int(cap))
+    if cap == 0 or not ranked:
+        return []
+    cands = list(dict.fromkeys(ranked))
+    cap = min(cap, len(cands))
+    cset = set(cands)
+    rank = {c: i for i, c in enumerate(cands)}
+    adj = defaultdict(set)
+    for a, b in pairs or ():
+        if a != b and a in cset and b in cset:
+            adj[a].add(b)
+            adj[b].add(a)
+    fraction = min(1.0, max(0.0, float(fraction)))
+    primary = max(1, min(cap, int(round(cap * (1.0 - fraction)))))
+    sel, sset = [], set()
+    rem = {c: set(adj.get(c, ())) for c in cands}
+    heap = [(-len(rem[c]), rank[c], c) for c in cands if rem[c]]
+    heapq.heapify(heap)
+    while len(sel) < primary and heap:
+        nd, _, c = heapq.heappop(heap)
+        if c in sset:
+            continue
+        live = len(rem[c])
+        if -nd != live:
+            heapq.heappush(heap, (-live, rank[c], c))
+            continue
+        if live == 0:
+            break
+        sel.append(c)
+        sset.add(c)
+        for nb in tuple(rem[c]):
+            rem[nb].discard(c)
+            heapq.heappush(heap, (-len(rem[nb]), rank[nb], nb))
+        rem[c].clear()
+    if len(sel) < primary:
+        nonred = [c for c in cands if c not in sset and not (adj.get(c, set()) & sset)]
+        nrs = set(nonred)
+        for c in nonred + [c for c in cands if c not in sset and c not in nrs]:
+            sel.append(c)
+            sset.add(c)
+            if len(sel) >= primary:
+                break
+    if len(sel) < cap:
+        rest = [c for c in cands if c not in sset]
+        rng.shuffle(rest)
+        sel.extend(rest[:cap - len(sel)])
+    return sel
+
+
+def _pair_combinations(members):
+    out = set()
+    s = sorted(members)
+    for i in range(len(s)):
+        for j in range(i + 1, len(s)):
+            out.add((s[i], s[j]))
+    return out
+
+
+class _ViaPools:
+    """Column / segment via pools on the host (small: Nx*Ny*(Nz-2))."""
+
+    def __init__(self, nx, ny, nz, col_cap=4, seg_cap=2):
+        self.nx, self.ny, self.nz = nx, ny, nz
+        self.segZ = nz - 2 if nz > 2 else 0
+        self.has_seg = nz > 2
+        self.col_cap = np.full((nx, ny), col_cap, dtype=np.int16)
+        self.col_use = np.zeros((nx, ny), dtype=np.int16)
+        self.col_pres = np.zeros((nx, ny), dtype=np.float32)
+        if self.has_seg:
+            self.seg_cap = np.full((nx, ny, self.segZ), seg_cap, dtype=np.int8)
+            self.seg_use = np.zeros((nx, ny, self.segZ), dtype=np.int16)
+            self.seg_pres = np.zeros((nx, ny, self.segZ), dtype=np.float32)
+            self.seg_prefix = np.zeros((nx, ny, self.segZ), dtype=np.float32)
+            self.seg_pres_via = None
+
+    def rebuild(self, paths, plane, nx):
+        """One column count per contiguous via run; its hull of segments
+        (``_accumulate_via_usage_for_path`` :4470-4546)."""
+        col = np.zeros((self.nx, self.ny), dtype=np.int16)
+        seg = np.zeros((self.nx, self.ny, self.segZ), dtype=np.int16) if self.has_seg else None
+        for p in paths:
+            if not p or len(p) < 2:
+                continue
+            a = np.asarray(p, dtype=np.int64)
+            z = a // plane
+            r = a % plane
+            via = (r[:-1] == r[1:]) & (z[:-1] != z[1:])
+            if not via.any():
+                continue
+            idx = np.flatnonzero(via)
+            # run starts: a via hop whose previous hop is not a via hop in the same column
+            start = np.ones(idx.size, dtype=bool)
+            start[1:] = ~((idx[1:] == idx[:-1] + 1) & (r[idx[1:]] == r[idx[:-1]]))
+            run_id = np.cumsum(start) - 1
+            xs = r[idx] % nx
+            ys = r[idx] // nx
+            zl = np.clip(np.minimum(z[idx], z[idx + 1]), 1, self.nz - 2)
+            zh = np.clip(np.maximum(z[idx], z[idx + 1]), 1, self.nz - 2)
+            for k in np.flatnonzero(start):
+                col[xs[k], ys[k]] += 1
+            if seg is not None:
+                nrun = int(run_id[-1]) + 1
+                lo = np.full(nrun, 1 << 30)
+                hi = np.full(nrun, -1)
+                np.minimum.at(lo, run_id, zl)
+                np.maximum.at(hi, run_id, zh)
+                rx = xs[start]
+                ry = ys[start]
+                for q in range(nrun):
+                    for zz in range(int(lo[q]), int(hi[q])):
+                        s = zz - 1
+                        if 0 <= s < self.segZ:
+                            seg[rx[q], ry[q], s] += 1
+        self.col_use[:] = col
+        if seg is not None:
+            self.seg_use[:] = seg
+
+    def update_presence(self, alpha=0.6, beta=0.4):
+        over = np.maximum(0, self.col_use - self.col_cap).astype(np.float32)
+        self.col_pres = alpha * over + beta * self.col_pres
+        if self.has_seg:
+            over = np.maximum(0, self.seg_use - self.seg_cap).astype(np.float32)
+            prev = self.seg_pres_via if self.seg_pres_via is not None else self.seg_pres
+            self.seg_pres_via = alpha * over + beta * prev
+            self.seg_pres = self.seg_pres_via.copy()
+            np.cumsum(self.seg_pres, axis=2, out=self.seg_prefix)
+
+    def spatial_overuse(self):
+        t = int(np.maximum(0, self.col_use - self.col_cap).sum())
+        if self.has_seg:
+            t += int(np.maximum(0, self.seg_use - self.seg_cap).sum())
+        return t
+
+
+# ------------------------------------------------------------------- router
+class PathFinderRouter:
+    """GB300 PathFinder router with the reference's Python API."""
+
+    def __init__(self, config: Optional[PathFinderConfig] = None, use_gpu: Optional[bool] = None,
+                 device: str = "cuda"):
+        require_cuda()
+        self.config = config or PathFinderConfig()
+        self.device = device
+        self.lattice: Optional[Lattice] = None
+        self.net_paths: Dict[str, List[int]] = {}
+        self.iteration = 0
+        self.trace = None
+        self.search_log = None
+        self.stats = {"searches": 0, "arcs": 0, "pops": 0, "search_s": 0.0}
+
+    # ------------------------------------------------------------- set-up
+    @staticmethod
+    def board_bounds(board):
+        """``_calc_bounds`` (:3266-3321): pads of nets with 2+ pads, +3 mm."""
+        xs, ys = [], []
+        for net in getattr(board, "nets", []) or []:
+            pads = getattr(net, "pads", []) or []
+            if len(pads) >= 2:
+                for p in pads:
+                    if getattr(p, "position", None) is not None:
+                        xs.append(p.position.x)
+                        ys.append(p.position.y)
+        if not xs:
+            if hasattr(board, "_kicad_bounds"):
+                b = board._kicad_bounds
+                return (b[0] - 3.0, b[1] - 3.0, b[2] + 3.0, b[3] + 3.0)
+            return (0, 0, 100, 100)
+        return (min(xs) - 3.0, min(ys) - 3.0, max(xs) + 3.0, max(ys) + 3.0)
+
+    @staticmethod
+    def assign_layer_axes(signal_layers, demand_h_pct, anchor_top_is_h=True):
+        """``assign_layer_axes_by_demand`` (board_analyzer.py:17-62)."""
+        n = len(signal_layers)
+        if n == 0:
+            return set(), set()
+        if n == 1:
+            return (set(signal_layers), set()) if demand_h_pct >= 0.5 else (set(), set(signal_layers))
+        h_goal = max(1, min(n - 1, int(round(n * float(demand_h_pct)))))
+        h, v = set(), set()
+        want_h = anchor_top_is_h
+        for layer in signal_layers:
+            if want_h and len(h) < h_goal:
+                h.add(layer)
+            else:
+                v.add(layer)
+            want_h = not want_h
+        while len(h) < h_goal and v:
+            mid = sorted(v)[len(v) // 2]
+            v.remove(mid)
+            h.add(mid)
+        while len(h) > h_goal and h:
+            mid = sorted(h)[len(h) // 2]
+            h.remove(mid)
+            v.add(mid)
+        return h, v
+
+    @classmethod
+    def demand_layer_directions(cls, board, layer_count):
+        """``preferred_layer_directions_for_board`` (board_analyzer.py:65-105)."""
+        ddx = ddy = 0.0
+        for net in getattr(board, "nets", ()) or ():
+            pads = getattr(net, "pads", ()) or ()
+            if len(pads) < 2:
+                continue
+            a, b = pads[0].position, pads[1].position
+            ddx += abs(float(b.x) - float(a.x))
+            ddy += abs(float(b.y) - float(a.y))
+        tot = ddx + ddy
+        pct = ddx / tot if tot > 1e-9 else 0.5
+        if os.environ.get("ORTHO_LATERAL_ALL", "0") == "1":
+            sig = list(range(int(layer_count)))
+        else:
+            sig = list(range(1, max(1, int(layer_count) - 1)))
+        h, _ = cls.assign_layer_axes(sig, pct)
+        dirs = ["h" if z in h else "v" for z in range(int(layer_count))]
+        if dirs:
+            dirs[0] = "v"
+        return dirs
+
+    def initialize_graph(self, board) -> bool:
+        cfg = self.config
+        bounds = self.board_bounds(board)
+        nz = int(getattr(board, "layer_count", None) or cfg.layer_count)
+        cfg.layer_count = nz
+        pitch = cfg.grid_pitch
+        gx0 = round(bounds[0] / pitch) * pitch
+        gy0 = round(bounds[1] / pitch) * pitch
+        gx1 = round(bounds[2] / pitch) * pitch
+        gy1 = round(bounds[3] / pitch) * pitch
+        nx = int((gx1 - gx0) / pitch) + 1
+        ny = int((gy1 - gy0) / pitch) + 1
+        dirs = cfg.preferred_layer_directions or self.demand_layer_directions(board, nz)
+        spacing = max(float(cfg.via_diameter) + float(cfg.clearance),
+                      float(cfg.via_drill) + float(cfg.min_hole_to_hole))
+        lat = Lattice(nx, ny, nz, pitch=pitch, layer_dirs=list(dirs), via_cost=cfg.via_cost,
+                      allow_any_layer_via=cfg.allow_any_layer_via,
+                      adjacent_via_step_scale=cfg.adjacent_via_step_scale, min_via_center_spacing=spacing,
+                      wrong_way_cost_multiplier=float(os.environ.get("ORTHO_WRONG_WAY",
+                                                                     cfg.wrong_way_cost_multiplier)))
+        self.initialize_lattice(lat, bounds)
+        return True
+
+    def initialize_lattice(self, lattice: Lattice, bounds=None):
+        """Build the device CSR and congestion state for a lattice."""
+        self.lattice = lattice
+        if bounds is None:
+            p = lattice.pitch
+            bounds = (0.0, 0.0, (lattice.nx - 1) * p, (lattice.ny - 1) * p)
+        self.bounds = bounds
+        self.g = DeviceGraph(lattice, device=self.device)
+        self.s = DeviceState(self.g)
+        self.ops = Ops(self.g, self.s)
+        L = lattice
+        self.nx, self.ny, self.nz = L.nx, L.ny, L.nz
+        self.plane = L.plane
+        self.N = L.num_nodes
+        self.E = self.g.E
+        self.pools = _ViaPools(L.nx, L.ny, L.nz)
+        self.node_use = np.zeros(self.N, dtype=np.int16)
+        self.owner = np.full(self.N, -1, dtype=np.int32)
+        self.members: Dict[int, Set[int]] = {}
+        self.node_history = np.zeros(self.N, dtype=np.float32)
+        self._hist_iter = None
+        self._hist_nodes: Set[int] = set()
+        self.layer_bias = np.ones(self.nz, dtype=np.float32)
+        self._layer_bias_ema = None
+        self.net_paths = {}
+        self.net_to_edges: Dict[str, List[int]] = {}
+        self.edge_to_nets = defaultdict(set)
+        self.net_id_map: Dict[str, int] = {}
+        dev = self.g.device
+        self._d_col_pres = torch.zeros((L.nx, L.ny), dtype=torch.float32, device=dev)
+        self._d_col_use = torch.zeros((L.nx, L.ny), dtype=torch.int16, device=dev)
+        self._d_col_cap = torch.from_numpy(self.pools.col_cap).to(dev)
+        if self.pools.has_seg:
+            self._d_seg_prefix = torch.zeros((L.nx, L.ny, self.pools.segZ), dtype=torch.float32, device=dev)
+            self._d_seg_use = torch.zeros((L.nx, L.ny, self.pools.segZ), dtype=torch.int16, device=dev)
+            self._d_seg_cap = torch.from_numpy(self.pools.seg_cap).to(dev)
+        self._d_disc = torch.zeros(self.nz * self.nz, dtype=torch.float64, device=dev)
+        cap = max(1 << 16, min(self.E, 1 << 24))
+        self._ov_idx = torch.empty(cap, dtype=torch.int32, device=dev)
+        self._ov_val = torch.empty(cap, dtype=torch.float32, device=dev)
+        self._ov_cnt = torch.zeros(1, dtype=torch.int32, device=dev)
+        self._reset_policy_state()
+
+    def initialize_state(self):
+        """Reset the congestion state and policy for a new job on the same lattice."""
+        s = self.s
+        for t in (s.present, s.present_ema, s.history, s.total_cost, s.live_static, s.path_node_use,
+                  s.owner_count, s.owner_xor, s.node_history):
+            t.zero_()
+        s.layer_bias.fill_(1.0)
+        s.use_layer_bias = False
+        self.pools = _ViaPools(self.nx, self.ny, self.nz)
+        self.node_use.fill(0)
+        self.owner.fill(-1)
+        self.members = {}
+        self.node_history.fill(0)
+        self._hist_iter = None
+        self._hist_nodes = set()
+        self.layer_bias = np.ones(self.nz, dtype=np.float32)
+        self._layer_bias_ema = None
+        self.net_paths = {}
+        self.net_to_edges = {}
+        self.edge_to_nets = defaultdict(set)
+        self.net_id_map = {}
+        self.iteration = 0
+        self._reset_policy_state()
+
+    def profile_reset(self):
+        self.ops.reset_counters()
+        self.stats = {"searches": 0, "arcs": 0, "pops": 0, "search_s": 0.0}
+
+    def profile_snapshot(self):
+        c = dict(self.ops.counters)
+        return {"launches": int(c["launches"]), "h2d_bytes": int(c["h2d_bytes"]), "d2h_bytes": int(c["d2h_bytes"]),
+                "search_launches": int(c["search_launches"]), "search_kernel_ms": float(c["search_ms"]),
+                "searches": self.stats["searches"], "arcs": self.stats["arcs"], "pops": self.stats["pops"]}
+
+    def _reset_policy_state(self):
+        self.stagnation_counter = 0
+        self.full_graph_fallback_count = 0
+        self._last_ripped: Set[str] = set()
+        self._freeze_pres_fac_until = 0
+        self._stagnation_victim_history: Set[str] = set()
+        self._stagnation_victim_cursor = 0
+        self._cleanup_move_counts = defaultdict(int)
+        self.freeze = False
+        self.physical_cleanup_started = False
+        self.barrel_count = 0
+        self.path_node_scores: Dict[str, int] = {}
+        self.path_node_pairs = set()
+        self.exact_pairs = set()
+        self.barrel_conflict_nets: Set[str] = set()
+        self.barrel_owner_nets: Set[str] = set()
+        self.barrel_victim_nets: Set[str] = set()
+        self.physical_scores = defaultdict(int)
+        self._net_clean_iters: Dict[str, int] = {}
+        self._last_reroute_iter: Dict[str, int] = {}
+        self._via_pool_keepers = {}
+        self._via_pool_member_state = {}
+        self._via_pool_keeper_stagnation = {}
+        self._last_hotset_size = 0
+        self._pres_fac_now = 1.0
+        self._present_pres_fac = 1.0
+
+    # ------------------------------------------------------------- helpers
+    def _net_id(self, name):
+        if name not in self.net_id_map:
+            self.net_id_map[name] = len(self.net_id_map)
+        return self.net_id_map[name]
+
+    def idx_to_coord(self, n):
+        z, r = divmod(int(n), self.plane)
+        y, x = divmod(r, self.nx)
+        return x, y, z
+
+    def _via_nodes(self, path):
+        nodes = set()
+        for u, v in zip(path, path[1:]):
+            zu, ru = divmod(int(u), self.plane)
+            zv, rv = divmod(int(v), self.plane)
+            if ru != rv or zu == zv:
+                continue
+            for z in range(min(zu, zv), max(zu, zv) + 1):
+                nodes.add(z * self.plane + ru)
+        return sorted(nodes)
+
+    def _overused(self):
+        """(arc ids, over values) of every arc with present > capacity (device compaction)."""
+        lib = self.ops.lib
+        cap = int(self._ov_idx.numel())
+        _lib.check(lib.ogr_overused_arcs(self.E, self.s.present.data_ptr(), self.s.capacity.data_ptr(),
+                                         self._ov_idx.data_ptr(), self._ov_val.data_ptr(), cap,
+                                         self._ov_cnt.data_ptr(), None), "ogr_overused_arcs")
+        n = int(self._ov_cnt.item())
+        if n > cap:
+            raise RuntimeError("overused-arc buffer too small")
+        idx = self._ov_idx[:n].cpu().numpy().astype(np.int64)
+        val = self._ov_val[:n].cpu().numpy()
+        order = np.argsort(idx)
+        return idx[order], val[order]
+
+    def _over_map(self):
+        idx, val = self._overused()
+        return dict(zip(idx.tolist(), val.tolist())), idx, val
+
+    # host mirrors of node state ------------------------------------------------
+    def _mark_nodes(self, name, path, sign):
+        nid = self._net_id(name)
+        nodes = np.unique(np.asarray(path, dtype=np.int64))
+        if sign > 0:
+            self.node_use[nodes] += 1
+        else:
+            self.node_use[nodes] = np.maximum(self.node_use[nodes] - 1, 0)
+        for n in self._via_nodes(path):
+            if sign > 0:
+                m = self.members.setdefault(n, set())
+                m.add(nid)
+                self.owner[n] = nid if len(m) == 1 else -2
+            else:
+                m = self.members.get(n)
+                if not m:
+                    self.owner[n] = -1
+                    continue
+                m.discard(nid)
+                if not m:
+                    self.members.pop(n, None)
+                    self.owner[n] = -1
+                elif len(m) == 1:
+                    self.owner[n] = next(iter(m))
+                else:
+                    self.owner[n] = -2
+
+    def _accumulate_history(self, nodes):
+        nodes = np.unique(np.asarray(list(nodes), dtype=np.int64))
+        if nodes.size == 0:
+            return
+        if self._hist_iter != self.iteration:
+            self._hist_iter = self.iteration
+            self._hist_nodes = set()
+        nodes = np.asarray([n for n in nodes if int(n) not in self._hist_nodes], dtype=np.int64)
+        if nodes.size == 0:
+            return
+        self.node_history[nodes] += np.float32(self.config.node_history_increment)
+        self._hist_nodes.update(map(int, nodes))
+        d = torch.from_numpy(nodes).to(self.g.device)
+        self.s.node_history[d] = torch.from_numpy(self.node_history[nodes]).to(self.g.device)
+
+    def _update_tracking(self, name, edges):
+        self._clear_tracking(name)
+        self.net_to_edges[name] = edges
+        for e in edges:
+            self.edge_to_nets[e].add(name)
+
+    def _clear_tracking(self, name):
+        if name in self.net_to_edges:
+            for e in self.net_to_edges[name]:
+                self.edge_to_nets[e].discard(name)
+            del self.net_to_edges[name]
+
+    # ------------------------------------------------------------- tallies
+    def _compute_overuse(self):
+        over_sum, over_cnt, _, _, _ = self.ops.tally(canonical_only=True)
+        return over_sum + self.pools.spatial_overuse(), over_cnt
+
+    def _path_node_overuse(self):
+        over = np.maximum(np.asarray(self.node_use, dtype=np.int64) - 1, 0)
+        return int(over.sum()), int(np.count_nonzero(over))
+
+    def _path_node_conflicts(self):
+        shared = self.node_use > 1
+        if not shared.any():
+            return set(), set(), {}
+        members = defaultdict(set)
+        scores = defaultdict(int)
+        for name, path in self.net_paths.items():
+            if not path:
+                continue
+            nodes = np.unique(np.asarray(path, dtype=np.int32))
+            for n in nodes[shared[nodes]]:
+                members[int(n)].add(name)
+                scores[name] += 1
+        pairs = set()
+        for m in members.values():
+            pairs |= _pair_combinations(m)
+        return pairs, set(members), dict(scores)
+
+    def _detect_barrels(self):
+        """Exact barrel conflicts + shared path nodes (``_detect_barrel_conflicts`` :10778-11111)."""
+        self.barrel_conflict_nets, self.barrel_owner_nets, self.barrel_victim_nets = set(), set(), set()
+        self.physical_scores = defaultdict(int)
+        self.exact_pairs = set()
+        id_to_name = {v: k for k, v in self.net_id_map.items()}
+        srcs, dsts, nids = [], [], []
+        for name, path in self.net_paths.items():
+            if not path or len(path) < 2:
+                continue
+            a = np.asarray(path, dtype=np.int64)
+            srcs.append(a[:-1])
+            dsts.append(a[1:])
+            nids.append(np.full(len(path) - 1, self.net_id_map[name], dtype=np.int64))
+        exact = 0
+        if srcs:
+            s = np.concatenate(srcs)
+            d = np.concatenate(dsts)
+            en = np.concatenate(nids)
+            so, do = self.owner[s], self.owner[d]
+            sc = (so != -1) & (so != en)
+            dc = (do != -1) & (do != en)
+            cm = sc | dc
+            exact = int(cm.sum())
+            if exact:
+                pos = np.flatnonzero(cm)
+                victims = set(map(int, en[pos]))
+                cnodes = np.unique(np.concatenate([s[sc], d[dc]]))
+                self._accumulate_history(cnodes)
+                owners = set()
+                for n in cnodes:
+                    owners.update(self.members.get(int(n), ()))
+                for p in pos:
+                    vid = int(en[p])
+                    for n, flag in ((int(s[p]), sc[p]), (int(d[p]), dc[p])):
+                        if not flag:
+                            continue
+                        for oid in self.members.get(n, ()):
+                            if oid == vid:
+                                continue
+                            vn, on = id_to_name.get(vid), id_to_name.get(oid)
+                            if vn is not None and on is not None:
+                                self.physical_scores[vn] += 1
+                                self.physical_scores[on] += 1
+                                self.exact_pairs.add(tuple(sorted((vn, on))))
+                self.barrel_victim_nets = {id_to_name[i] for i in victims if i in id_to_name}
+                self.barrel_owner_nets = {id_to_name[i] for i in owners if i in id_to_name}
+                self.barrel_conflict_nets = {id_to_name[i] for i in (victims | owners) if i in id_to_name}
+        pairs, shared, pscores = self._path_node_conflicts()
+        self.path_node_pairs = set(pairs)
+        self.path_node_scores = dict(pscores)
+        if shared:
+            for name, sc_ in pscores.items():
+                self.physical_scores[name] += int(sc_)
+            self.barrel_conflict_nets.update({n for p in pairs for n in p})
+            self._accumulate_history(shared)
+        return exact + len(shared)
+
+    # ------------------------------------------------------------- device steps
+    def _upload_pools(self, pres_fac, penalty, block):
+        P = self.pools
+        dev = self.g.device
+        if penalty:
+            self._d_col_pres.copy_(torch.from_numpy(np.ascontiguousarray(P.col_pres)))
+            if P.has_seg:
+                self._d_seg_prefix.copy_(torch.from_numpy(np.ascontiguousarray(P.seg_prefix)))
+            lb = self.layer_bias
+            k = 0.20
+            zs = np.arange(self.nz)
+            sb = lb[zs]
+            disc = (1.0 - k * np.maximum(sb, 0.0))[:, None] * (1.0 + 0.5 * k * np.maximum(lb[zs], 0.0))[None, :]
+            self._d_disc.copy_(torch.from_numpy(np.asarray(disc, dtype=np.float64).ravel()))
+        if block:
+            self._d_col_use.copy_(torch.from_numpy(np.ascontiguousarray(P.col_use)))
+            if P.has_seg:
+                self._d_seg_use.copy_(torch.from_numpy(np.ascontiguousarray(P.seg_use)))
+        g = self.g
+        seg = P.has_seg
+        _lib.check(self.ops.lib.ogr_via_pools_apply(
+            self.E, self.nx, self.ny, self.nz, g.edge_src.data_ptr(), g.indices.data_ptr(), g.edge_kind.data_ptr(),
+            self._d_col_pres.data_ptr(), self._d_seg_prefix.data_ptr() if seg else None,
+            self._d_col_use.data_ptr(), self._d_col_cap.data_ptr(),
+            self._d_seg_use.data_ptr() if seg else None, self._d_seg_cap.data_ptr() if seg else None,
+            self._d_disc.data_ptr(), float(np.float32(1.0)), float(np.float32(1.0)), float(np.float32(pres_fac)),
+            int(bool(penalty)), int(bool(block)), self.s.total_cost.data_ptr(), None), "ogr_via_pools_apply")
+
+    def _layer_bias_for_costs(self):
+        """``_compute_layer_bias`` (:8451-8534) from exact device tallies."""
+        _, _, _, _, units = self.ops.tally(canonical_only=True)
+        per_layer = units.astype(np.float64) / float(1 << 23)
+        maxv = float(per_layer.max())
+        if maxv <= 1e-9:
+            raw = np.ones(self.nz, dtype=np.float32)
+        else:
+            raw = 1.0 + 0.75 * (per_layer / maxv)
+        if self._layer_bias_ema is None:
+            self._layer_bias_ema = raw.astype(np.float32)
+        else:
+            self._layer_bias_ema = (0.88 * self._layer_bias_ema + (1.0 - 0.88) * raw).astype(np.float32)
+        self._layer_bias_ema = np.clip(self._layer_bias_ema, 1.0, 1.80)
+        return self._layer_bias_ema
+
+    # ------------------------------------------------------------- routing
+    def _search(self, name, src, dst, bonus, full_graph):
+        cfg = self.config
+        radius = max(60, int(self._manhattan(src, dst) * 0.75 + bonus * 2.0))
+        net = self.ops.net_args(
+            self._net_id(name), src, dst, full_graph=full_graph,
+            max_depth=min(int(radius + bonus * 2.0), 80), halo=min(16, 2 + int(max(0.0, bonus) / 0.6)),
+            max_roi_nodes=MAX_ROI_NODES, pres_fac=self._pres_fac_now, owner_base=cfg.owner_penalty_base,
+            path_base=cfg.path_node_penalty_base, hist_pen=cfg.node_history_penalty,
+            freeze_weight=cfg.portal_cleanup_node_penalty if self.freeze else None, penalty=True)
+        t = time.perf_counter()
+        path = self.ops.find_path(net)
+        self.stats["search_s"] += time.perf_counter() - t
+        self.stats["searches"] += 1
+        st = self.ops.stats.cpu().numpy()
+        self.stats["arcs"] += int(st[0])
+        self.stats["pops"] += int(st[1])
+        self.ops.stats.zero_()
+        return path
+
+    def _manhattan(self, s, d):
+        sx, sy, _ = self.idx_to_coord(s)
+        dx, dy, _ = self.idx_to_coord(d)
+        return abs(dx - sx) + abs(dy - sy)
+
+    def _apply(self, name, path, sign, live):
+        edges = self.ops.apply_path(path, self._net_id(name), sign, self._present_pres_fac, live=live)
+        self._mark_nodes(name, path, sign)
+        return edges
+
+    def _order_nets(self, tasks):
+        over_map, _, _ = self._over_map()
+        scores = []
+        for name, (s, d) in tasks.items():
+            sx, sy, sz = self.idx_to_coord(s)
+            dx, dy, dz = self.idx_to_coord(d)
+            dist = abs(dx - sx) + abs(dy - sy) + abs(dz - sz)
+            cong = 0.0
+            if name in self.net_to_edges:
+                edges = self.net_to_edges[name]
+                cong = sum(float(over_map.get(e, 0.0)) for e in edges) / max(1, len(edges))
+            scores.append((dist * 3 * (cong + 1), name))
+        owners, victims = self.barrel_owner_nets, self.barrel_victim_nets
+        scores.sort(key=lambda it: (2 if it[1] in owners and it[1] not in victims else 1 if it[1] in owners else 0,
+                                    it[0], it[1]), reverse=True)
+        rotation = 0
+        if not owners and not victims:
+            rotation = random.Random(42 + int(self.iteration)).randint(0, min(5, len(scores) // 10))
+        ordered = [n for _, n in scores]
+        if rotation > 0:
+            ordered = ordered[rotation:] + ordered[:rotation]
+        return ordered
+
+    def _route_all(self, tasks, all_tasks):
+        cfg = self.config
+        self.full_graph_fallback_count = 0
+        bonus = self.stagnation_counter * 0.6
+        ordered = self._order_nets(tasks)
+        live = bool(cfg.live_present_costs)
+        if live:
+            self.ops.live_begin(self._present_pres_fac)
+        for name in ordered:
+            src, dst = tasks[name]
+            if name in self.net_paths and self.net_paths[name]:
+                self._apply(name, self.net_paths[name], -1, live)
+                self._clear_tracking(name)
+            full = self._manhattan(src, dst) >= ROI_THRESHOLD_STEPS
+            path = self._search(name, src, dst, bonus, full)
+            if self.search_log is not None:
+                self.search_log.append((self.iteration, name, "full" if full else "roi", path))
+            if (not path or len(path) <= 1) and self.full_graph_fallback_count < 5:
+                path = self._search(name, src, dst, bonus * 2, False)
+                if self.search_log is not None:
+                    self.search_log.append((self.iteration, name, "fallback", path))
+                self.full_graph_fallback_count += 1
+            if path and len(path) > 1:
+                edges = self._apply(name, path, +1, live)
+                self.net_paths[name] = path
+                self._update_tracking(name, edges)
+            else:
+                self.net_paths[name] = []
+                self._clear_tracking(name)
+        routed = sum(1 for p in self.net_paths.values() if p)
+        return routed, len(all_tasks) - routed
+
+    # ------------------------------------------------------------- hotset
+    def _via_keeper_threshold(self):
+        routed = sum(bool(p) for p in self.net_paths.values())
+        step = max(1, int(self.config.via_keeper_rotation_nets_per_step))
+        return max(0, int(self.config.via_keeper_rotation_overuse_threshold)) * max(1, int(np.ceil(routed / step)))
+
+    def _find_via_pool_offenders(self):
+        P = self.pools
+        col_over = P.col_use > P.col_cap
+        col_over = col_over if np.any(col_over) else None
+        seg_over = None
+        if P.has_seg:
+            m = P.seg_use > P.seg_cap
+            seg_over = m if np.any(m) else None
+        if col_over is None and seg_over is None:
+            self._via_pool_keepers, self._via_pool_member_state, self._via_pool_keeper_stagnation = {}, {}, {}
+            return set()
+        members = defaultdict(set)
+        for name, path in self.net_paths.items():
+            if not path or len(path) < 2:
+                continue
+            res = set()
+            for u, v in zip(path, path[1:]):
+                xu, yu, zu = self.idx_to_coord(u)
+                xv, yv, zv = self.idx_to_coord(v)
+                if xu != xv or yu != yv or zu == zv:
+                    continue
+                if col_over is not None and col_over[xu, yu]:
+                    res.add(("col", xu, yu))
+                if seg_over is not None:
+                    zl = max(1, min(min(zu, zv), self.nz - 2))
+                    zh = max(1, min(max(zu, zv), self.nz - 2))
+                    for z in range(zl, zh):
+                        if 0 <= z - 1 < P.segZ and seg_over[xu, yu, z - 1]:
+                            res.add(("seg", xu, yu, z - 1))
+            for r in res:
+                members[r].add(name)
+        rotation_allowed = P.spatial_overuse() <= self._via_keeper_threshold()
+        nk, nm, ns, off = {}, {}, {}, set()
+        for r, mem in sorted(members.items()):
+            kind, x, y, *tail = r
+            if kind == "col":
+                capv, obs = int(P.col_cap[x, y]), int(P.col_use[x, y])
+            else:
+                capv, obs = int(P.seg_cap[x, y, tail[0]]), int(P.seg_use[x, y, tail[0]])
+            capv = max(0, capv)
+            state = frozenset(mem)
+            nm[r] = state
+            stagn = int(self._via_pool_keeper_stagnation.get(r, 0)) + 1 \
+                if self._via_pool_member_state.get(r) == state else 0
+            prev = [n for n in self._via_pool_keepers.get(r, ()) if n in mem][:capv]
+            remaining = sorted(mem - set(prev))
+            keepers = tuple(prev + remaining[:max(0, capv - len(prev))])
+            if rotation_allowed and stagn >= 2 and 0 < capv < len(mem) and prev:
+                ordered = sorted(mem)
+                st0 = (ordered.index(prev[0]) + 1) % len(ordered)
+                keepers = tuple(ordered[(st0 + o) % len(ordered)] for o in range(capv))
+                stagn = 0
+            ns[r] = stagn
+            nk[r] = keepers
+            off.update(mem - set(keepers))
+            if obs > len(mem):
+                off.update(mem)
+        self._via_pool_keepers, self._via_pool_member_state, self._via_pool_keeper_stagnation = nk, nm, ns
+        return off
+
+    def _effective_cap(self, t):
+        cfg = self.config
+        base = _history_hotset_cap(t)
+        if t > int(cfg.slow_progress_min_overuse) and self.iteration <= int(getattr(self, "_hotset_rate_boost_until", 0)):
+            init = max(1, int(cfg.slow_progress_hotset_cap))
+            mx = max(init, int(cfg.slow_progress_hotset_cap_max))
+            ga = max(1, int(cfg.slow_progress_hotset_growth_after))
+            ev = max(1, int(getattr(self, "_slow_progress_event_count", 1)))
+            return max(base, min(mx, init * (2 ** max(0, ev - ga + 1))))
+        return base
+
+    def _bounded_cap(self, t):
+        base = _history_hotset_cap(t)
+        eff = self._effective_cap(t)
+        conf = max(1, int(self.config.hotset_cap))
+        if eff > base:
+            conf = max(conf, eff)
+        cap = min(conf, eff)
+        floor = int(self.config.hotset_cap_floor)
+        if floor > 0 and t > 2048:
+            cap = max(cap, floor)
+        return cap
+
+    def _physical_hotset(self):
+        off = set(self.barrel_conflict_nets)
+        cfg = self.config
+        mx = max(1, int(cfg.physical_hotset_cap))
+        mn = min(mx, max(1, int(cfg.physical_hotset_min)))
+        scale = max(1.0, float(cfg.physical_conflicts_per_hotset_net))
+        cap = min(mx, max(mn, int(np.ceil(max(0, self.barrel_count) / scale))))
+        if len(off) <= cap:
+            return off
+        return set(sorted(off, key=lambda n: (-int(self.physical_scores.get(n, 0)), str(n)))[:cap])
+
+    def _build_hotset(self, tasks, ripped):
+        over_map, over_idx_arr, _ = self._over_map()
+        over_idx = set(over_idx_arr.tolist())
+        via_off = self._find_via_pool_offenders()
+        pscores = {n: int(s) for n, s in self.path_node_scores.items() if n in tasks and int(s) > 0}
+        poff = set(pscores)
+        total_neg = self._compute_overuse()[0] + self._path_node_overuse()[0]
+        thr = int(self.config.portal_cleanup_edge_threshold)
+        if self.config.physical_cleanup_overuse_threshold is not None:
+            thr = max(thr, int(self.config.physical_cleanup_overuse_threshold))
+        if not over_idx:
+            unrouted = {n for n in tasks if not self.net_paths.get(n)}
+            phys = self._physical_hotset() if total_neg <= thr else set()
+            hot = unrouted | ripped | via_off | phys
+            hot.update(_conflict_aware_hotset(sorted(poff, key=lambda n: (-pscores[n], str(n))), self.path_node_pairs,
+                                              self._bounded_cap(total_neg), _exploration_fraction(total_neg),
+                                              random.Random(42 + self.iteration)))
+            self._last_hotset_size = len(hot)
+            return hot
+        offenders = set()
+        for e in over_idx:
+            offenders.update(self.edge_to_nets.get(e, set()))
+        offenders.update(poff)
+        for n in tasks:
+            self._net_clean_iters[n] = 0 if n in offenders else self._net_clean_iters.get(n, 0) + 1
+        offenders -= {n for n in offenders if self._net_clean_iters.get(n, 0) >= 3}
+        offenders |= ripped
+        offenders |= via_off
+        unrouted = {n for n in tasks if not self.net_paths.get(n)}
+        scores = []
+        for n in offenders:
+            imp = float(pscores.get(n, 0))
+            if n in self.net_to_edges:
+                imp += sum(float(over_map[e]) for e in self.net_to_edges[n] if e in over_idx)
+            scores.append((imp, n))
+        for n in unrouted:
+            if n not in offenders:
+                scores.append((0.0, n))
+        scores.sort(reverse=True)
+        cap = self._bounded_cap(total_neg)
+        rng = random.Random(42 + self.iteration)
+        ranked = [n for _, n in scores if self.iteration - self._last_reroute_iter.get(n, -999) > 1]
+        sel = _conflict_aware_hotset(ranked, self.path_node_pairs, cap, _exploration_fraction(total_neg), rng)
+        for n in sel:
+            self._last_reroute_iter[n] = self.iteration
+        hot = set(sel)
+        if len(over_idx) <= thr and total_neg <= thr:
+            hot.update(self._physical_hotset())
+        hot.update(unrouted)
+        self._last_hotset_size = len(hot)
+        return hot
+
+    # ------------------------------------------------------------- state
+    def _capture(self):
+        return {n: list(p) for n, p in self.net_paths.items()}
+
+    def _restore(self, state):
+        """``_restore_routing_state`` (:7806-7838): re-commit every path."""
+        self.net_paths.clear()
+        self.net_paths.update({n: list(p) for n, p in state.items()})
+        self.s.present.zero_()
+        self.s.path_node_use.zero_()
+        self.s.owner_count.zero_()
+        self.s.owner_xor.zero_()
+        self.node_use.fill(0)
+        self.owner.fill(-1)
+        self.members = {}
+        self.net_to_edges.clear()
+        self.edge_to_nets.clear()
+        for n, p in self.net_paths.items():
+            if not p or len(p) < 2:
+                continue
+            edges = self._apply(n, p, +1, live=False)
+            self._update_tracking(n, edges)
+        self._rebuild_via_usage()
+
+    def _rebuild_via_usage(self):
+        self.pools.rebuild(list(self.net_paths.values()), self.plane, self.nx)
+
+    def _rip_top_k(self, k=20):
+        over_map, over_idx_arr, _ = self._over_map()
+        canon = [int(e) for e in over_idx_arr.tolist() if self._arc_is_canonical(int(e))]
+        over_idx = set(canon)
+        _, _, mscores = self._path_node_conflicts()
+        self.path_node_scores = dict(mscores)
+        cands = set(mscores)
+        for e in over_idx:
+            cands.update(self.edge_to_nets.get(e, ()))
+        scores = []
+        for n in cands:
+            if not self.net_paths.get(n):
+                continue
+            imp = float(mscores.get(n, 0))
+            if n in self.net_to_edges:
+                imp += sum(float(over_map[e]) for e in self.net_to_edges[n] if e in over_idx)
+            if imp > 0:
+                scores.append((imp, n))
+        scores.sort(key=lambda it: (-it[0], str(it[1])))
+        ranked = [n for _, n in scores]
+        victims = set()
+        if ranked and k > 0:
+            if not self._stagnation_victim_history:
+                self._stagnation_victim_cursor = 0
+            cnt = min(int(k), len(ranked))
+            start = int(self._stagnation_victim_cursor) % len(ranked)
+            victims = {ranked[(start + o) % len(ranked)] for o in range(cnt)}
+            self._stagnation_victim_cursor = (start + cnt) % len(ranked)
+            self._stagnation_victim_history = victims
+        for n in victims:
+            if self.net_paths.get(n) and n in self.net_to_edges:
+                self._apply(n, self.net_paths[n], -1, live=False)
+                self.net_paths[n] = []
+                self._clear_tracking(n)
+        return victims
+
+    def _arc_is_canonical(self, e):
+        return int(self._edge_src_host[e]) < int(self._indices_host[e])
+
+    def _movable_components(self, pairs):
+        adj = defaultdict(set)
+        for a, b in pairs:
+            if a != b:
+                adj[a].add(b)
+                adj[b].add(a)
+        movable, eligible = set(), set(adj)
+        while eligible:
+            n = min(eligible, key=lambda c: (self._cleanup_move_counts[c], -len(adj[c]), c))
+            movable.add(n)
+            eligible.discard(n)
+            eligible.difference_update(adj[n])
+        for n in movable:
+            self._cleanup_move_counts[n] += 1
+        return movable
+
+    def _layer_congestion(self, idx, val):
+        if idx.size == 0:
+            return {}
+        lays = self._edge_layer_host[idx]
+        out = {}
+        for z in range(1, self.nz + 1):
+            m = lays == z
+            if np.any(m):
+                out[z] = float(np.sum(val[m]))
+        return out
+
+    # ------------------------------------------------------------- public API
+    def _parse_requests(self, requests):
+        tasks = {}
+        for r in requests:
+            if isinstance(r, tuple) and len(r) == 3:
+                tasks[str(r[0])] = (int(r[1]), int(r[2]))
+            else:
+                raise TypeError("requests must be (name, src_node, dst_node) tuples")
+        return tasks
+
+    def route_multiple_nets(self, requests, progress_cb=None, iteration_cb=None) -> Dict:
+        if self.lattice is None:
+            raise RuntimeError("initialize_graph() first")
+        tasks = self._parse_requests(requests)
+        self._edge_src_host = self.g.edge_src.cpu().numpy()
+        self._indices_host = self.g.indices.cpu().numpy()
+        self._edge_layer_host = self.g.edge_layer.cpu().numpy()
+        self._edge_kind_host = self.g.edge_kind.cpu().numpy().astype(bool)
+        return self._negotiate(tasks, progress_cb, iteration_cb)
+
+    def _derive(self, tasks):
+        """``analyze_board_characteristics`` + ``derive_routing_parameters`` +
+        ``apply_derived_parameters`` (board_analyzer.py:151-305,
+        parameter_derivation.py:51-278)."""
+        cfg = self.config
+        pitch = self.lattice.pitch
+        width = self.bounds[2] - self.bounds[0]
+        height = self.bounds[3] - self.bounds[1]
+        nsig = max(0, self.nz - 2)
+        chans = nsig * int(width / pitch) * int(height / pitch)
+        hpwl = 0.0
+        for _, (s, d) in tasks.items():
+            sx, sy, _ = self.idx_to_coord(s)
+            dx, dy, _ = self.idx_to_coord(d)
+            hpwl += abs(dx - sx) * pitch + abs(dy - sy) * pitch
+        rho = (hpwl * 1.3) / max(1.0, chans * pitch * 0.75)
+        L, N = nsig, len(tasks)
+        if rho < 0.6:
+            mult, pmax = 1.15, 6.0
+        elif rho < 0.9:
+            mult, pmax = 1.12, 7.0
+        elif rho < 1.2:
+            mult, pmax = 1.10, 8.0
+        else:
+            mult, pmax = 1.08, 10.0
+        pmax *= 0.75 if L <= 12 else 1.25 if L >= 25 else 1.0
+        bonus = 6.0 if L <= 10 else 4.0 if L <= 15 else 2.0 if L <= 25 else 0.0
+        pct = 0.25 if rho < 0.7 else 0.20 if rho < 1.0 else 0.15 if rho < 1.3 else 0.12
+        patience = 5 if rho < 0.8 else 6 if rho < 1.1 else 8
+        if L <= 12:
+            patience = max(patience, 7)
+        cfg.pres_fac_init, cfg.pres_fac_mult, cfg.pres_fac_max = 1.0, mult, pmax
+        cfg.hist_cost_weight = 8.0 + bonus + 6.0 * max(0.0, min(1.0, rho - 0.7))
+        cfg.hist_gain = 0.20 + 0.15 * max(0.0, min(1.0, rho - 0.8))
+        cfg.history_decay = 1.0
+        cfg.hotset_cap = max(32, min(int(N * pct), int(N * 0.30)))
+        cfg.via_cost = 0.5
+        cfg.stagnation_patience = patience
+        if "max_iterations" not in cfg._explicit:
+            cfg.max_iterations = max(cfg.max_iterations, 250)
+
+    def _negotiate(self, tasks, progress_cb=None, iteration_cb=None):
+        cfg = self.config
+        self._derive(tasks)
+        nsig = self.nz - 2
+        pres_fac = float(cfg.pres_fac_init)
+        pres_mult = float(os.getenv('ORTHO_PRES_FAC_MULT', cfg.pres_fac_mult))
+        hist_gain = float(os.getenv('ORTHO_HIST_GAIN', cfg.hist_gain))
+        hw_mult = 1.2 if nsig <= 12 else 1.0 if nsig <= 20 else 0.8
+        floor = 32.0 if nsig <= 12 else 64.0 if nsig <= 20 else 128.0
+        pres_max = float(os.getenv('ORTHO_PRES_FAC_MAX', max(float(cfg.pres_fac_max), floor)))
+        hist_decay = float(os.getenv("ORTHO_HISTORY_DECAY",
+                                     cfg.history_decay if cfg.history_decay is not None else 1.0))
+        best_overuse, best_score, best_state, best_iter = float('inf'), None, None, 0
+        stagnant = 0
+        neg_hist = []
+        self._slow_progress_event_count = 0
+        self._hotset_rate_boost_until = 0
+        last_slow = -1_000_000
+        trial_ref_ceiling = trial_ref_frac = None
+        trial_under = 0
+        adaptive_limit = float(cfg.slow_progress_pres_fac_max)
+        metrics = []
+        jam = None
+        failed = over_sum = over_cnt = negotiated = conflicts = 0
+        t_start = time.time()
+        s = self.s
+        for it in range(1, cfg.max_iterations + 1):
+            self.iteration = it
+            t_it = time.time()
+            self._pres_fac_now = pres_fac
+            self._rebuild_via_usage()
+            self.pools.update_presence()
+            if it == 1:
+                s.present_ema.copy_(s.present)
+            self.ops.present_ema(0.40)
+            lb = self._layer_bias_for_costs()
+            vmult = 1.0
+            if it >= 3 and self.pools.spatial_overuse() >= int(cfg.via_pressure_threshold):
+                vmult = float(cfg.via_pressure_multiplier)
+            elif pres_fac >= 64:
+                _, idx, val = self._over_map()
+                vo = float(val[self._edge_kind_host[idx]].sum()) if idx.size else 0.0
+                to = float(val.sum())
+                if to > 0:
+                    vmult = 1.5 if vo / to > 0.7 else 0.5
+            self.ops.update_costs(pres_fac, cfg.hist_cost_weight * hw_mult, vmult, cfg.base_cost_weight, lb)
+            self._present_pres_fac = pres_fac
+            self._upload_pools(pres_fac, penalty=True, block=it > 1)
+            if cfg.reroute_only_offenders and it > 1:
+                hot = self._build_hotset(tasks, self._last_ripped)
+                sub = {k: v for k, v in tasks.items() if k in hot}
+                self._last_ripped = set()
+            else:
+                sub = dict(tasks)
+            work_scale = min(max(1.0, float(cfg.pressure_work_scale_max)),
+                             max(1.0, len(sub) / max(1, int(cfg.pressure_reference_hotset)))) if it > 1 else 1.0
+            routed, failed = self._route_all(sub, tasks)
+            conflicts = self._detect_barrels()
+            self.barrel_count = conflicts
+            over_sum, over_cnt = self._compute_overuse()
+            pno, _ = self._path_node_overuse()
+            negotiated = over_sum + pno
+            clean = over_sum == 0 and pno == 0
+            thr = int(cfg.portal_cleanup_edge_threshold)
+            if conflicts > 0 and over_cnt <= thr and negotiated <= thr:
+                self._last_ripped = set(self._last_ripped) | set(self.barrel_conflict_nets)
+            gate = thr if cfg.physical_cleanup_overuse_threshold is None else \
+                max(thr, int(cfg.physical_cleanup_overuse_threshold))
+            if conflicts > 0 and over_cnt <= gate and negotiated <= gate:
+                if not self.freeze:
+                    self.physical_cleanup_started = True
+                self.freeze = True
+                mov = self._movable_components(set(self.exact_pairs) | set(self.path_node_pairs))
+                if mov:
+                    self.barrel_conflict_nets = set(mov)
+                    self._last_ripped = set(mov)
+            elif conflicts == 0:
+                self.freeze = False
+                self._cleanup_move_counts.clear()
+            elif self.freeze and (over_cnt > thr or negotiated > thr):
+                self.freeze = False
+            metrics.append({'iter': it, 'nets_routed': routed, 'overuse_sum': over_sum, 'overuse_edges': over_cnt,
+                            'iter_time_s': round(time.time() - t_it, 4),
+                            'total_time_s': round(time.time() - t_start, 4)})
+            if self.trace is not None:
+                self.trace.append(self._capture())
+            score = (int(failed), int(over_sum) + int(pno), int(conflicts))
+            if best_score is None or score < best_score:
+                best_score, best_state, best_iter = score, self._capture(), it
+                self._stagnation_victim_history = set()
+                self._stagnation_victim_cursor = 0
+            neg_hist.append(negotiated)
+            window = max(1, int(cfg.slow_progress_window))
+            slow, frac = self._rolling(neg_hist, window)
+            if slow and it - last_slow >= window:
+                last_slow = it
+                self._slow_progress_event_count += 1
+                self._hotset_rate_boost_until = it + window
+                after = max(1, int(cfg.slow_progress_pressure_after))
+                old_ceiling = pres_max
+                rejected = None
+                if (self._slow_progress_event_count >= 4 and self._last_hotset_size >= int(cfg.slow_progress_hotset_cap_max)
+                        and frac is not None):
+                    trial_ref_ceiling, trial_ref_frac, trial_under, rejected = self._pressure_trial(
+                        old_ceiling, frac, trial_ref_ceiling, trial_ref_frac, trial_under)
+                    if rejected is not None:
+                        adaptive_limit = min(adaptive_limit, float(trial_ref_ceiling))
+                        pres_max = min(pres_max, adaptive_limit)
+                        pres_fac = min(pres_fac, pres_max)
+                if self._slow_progress_event_count >= after and rejected is None:
+                    mx = min(float(cfg.slow_progress_pres_fac_max), adaptive_limit)
+                    pres_max = min(max(old_ceiling, mx), max(128.0, old_ceiling * 2.0))
+                    pres_fac = min(pres_fac * 1.5, pres_max)
+            if over_sum > 0:
+                _, oidx, oval = self._over_map()
+                by_layer = self._layer_congestion(oidx, oval)
+                if by_layer and sum(by_layer.values()) > 0:
+                    lo = np.array([by_layer.get(z, 0.0) for z in range(self.nz)])
+                    mean = np.mean(lo[lo > 0]) + 1e-9
+                    alpha, bmin, bmax = (0.20, 0.60, 1.80) if nsig <= 12 else \
+                        (0.12, 0.75, 1.50) if nsig <= 20 else (0.08, 0.85, 1.20)
+                    target = 1.0 + alpha * (lo / mean - 1.0)
+                    self.layer_bias = np.clip(0.85 * self.layer_bias + 0.15 * target, bmin, bmax)
+                    tot = sum(by_layer.values())
+                    mz, mo = max(by_layer.items(), key=lambda x: x[1])
+                    if jam is None:
+                        jam = {'layer': None, 'count': 0, 'boost_until': 0}
+                    if (mo / tot) * 100 >= 60.0:
+                        if jam['layer'] == mz:
+                            jam['count'] += 1
+                        else:
+                            jam = {'layer': mz, 'count': 1, 'boost_until': 0}
+                        if jam['count'] >= 3 and it > jam['boost_until']:
+                            self.layer_bias[mz] = min(self.layer_bias[mz] * 1.8, bmax)
+                            jam['boost_until'] = it + 3
+                    else:
+                        jam = {'layer': None, 'count': 0, 'boost_until': 0}
+            if clean:
+                pres_fac = min(pres_fac, 10.0)
+            hg = min(1.2, hist_gain * 1.25) if (it >= 8 and over_sum > 0) else hist_gain
+            use_cap = os.getenv('ORTHO_NO_HISTORY_CAP', '0') == '0'
+            self.ops.update_history(hg, cap_mult=15.0 if use_cap else 1.0, decay=hist_decay, use_cap=use_cap,
+                                    use_raw_present=True)
+            if progress_cb:
+                try:
+                    progress_cb(it, cfg.max_iterations, f"Iteration {it}")
+                except Exception:
+                    pass
+            if iteration_cb:
+                try:
+                    iteration_cb(it, [], [], over_sum, over_cnt)
+                except Exception:
+                    pass
+            if failed == 0 and clean:
+                bc = self._detect_barrels()
+                self.barrel_count = bc
+                if bc == 0:
+                    return {'success': True, 'converged': True, 'paths': self.net_paths, 'iterations': it,
+                            'barrel_conflicts': 0, 'overuse_sum': 0, 'overuse_edges': 0, 'failed_nets': 0,
+                            'iteration_metrics': metrics, 'total_time_s': round(time.time() - t_start, 4)}
+            if negotiated < best_overuse:
+                best_overuse, stagnant = negotiated, 0
+            else:
+                stagnant += 1
+            if stagnant == 2:
+                pres_fac = min(pres_fac * 1.5, pres_max)
+            if stagnant >= cfg.stagnation_patience and it < cfg.max_iterations:
+                if self.physical_cleanup_started or self.pools.spatial_overuse() > self._via_keeper_threshold():
+                    stagnant = 0
+                else:
+                    cur = (int(failed), int(over_sum) + int(pno), int(conflicts))
+                    if best_state is not None and best_score is not None and best_score < cur:
+                        self._restore(best_state)
+                    self.stagnation_counter += 1
+                    self._last_ripped = self._rip_top_k(20)
+                    self._freeze_pres_fac_until = it + 2
+                    stagnant = 0
+                    continue
+            if it > self._freeze_pres_fac_until:
+                pres_fac = min(pres_fac * (pres_mult ** work_scale), pres_max)
+        cur = (int(failed), int(over_sum) + self._path_node_overuse()[0], int(self.barrel_count))
+        restored = best_state is not None and best_score is not None and best_score < cur
+        if restored:
+            self._restore(best_state)
+            failed = sum(1 for n in tasks if not self.net_paths.get(n))
+            over_sum, over_cnt = self._compute_overuse()
+            self.barrel_count = self._detect_barrels()
+            negotiated = over_sum + self._path_node_overuse()[0]
+        if 0 < negotiated <= 100:
+            det = self._detail_pass(tasks, negotiated, pres_max)
+            if det.get('success'):
+                det['iteration_metrics'] = metrics
+                det['best_iteration'] = best_iter
+                return det
+        final_barrels = self._detect_barrels()
+        success = failed == 0 and over_sum == 0 and final_barrels == 0
+        return {'success': success, 'converged': success, 'barrel_conflicts': final_barrels,
+                'overuse_sum': over_sum, 'overuse_edges': over_cnt, 'failed_nets': failed,
+                'path_node_overuse_sum': self._path_node_overuse()[0], 'nets_routed': len(tasks) - failed,
+                'total_nets': len(tasks), 'iterations': len(metrics), 'best_iteration': best_iter,
+                'restored_best_state': restored, 'iteration_metrics': metrics, 'paths': self.net_paths,
+                'total_time_s': round(time.time() - t_start, 4)}
+
+    def _rolling(self, values, window):
+        cfg = self.config
+        if len(values) < window + 1:
+            return False, None
+        start = float(values[-window - 1])
+        if start <= max(0, int(cfg.slow_progress_min_overuse)):
+            return False, None
+        frac = max(0.0, (start - min(map(float, values[-window:]))) / max(1.0, start))
+        return frac < max(0.0, float(cfg.slow_progress_min_fraction)), frac
+
+    def _pressure_trial(self, cur_ceiling, cur_frac, ref_ceiling, ref_frac, under):
+        cfg = self.config
+        ceiling, frac = float(cur_ceiling), max(0.0, float(cur_frac))
+        if ref_ceiling is None or ref_frac is None:
+            return ceiling, frac, 0, None
+        pc, pf = float(ref_ceiling), max(0.0, float(ref_frac))
+        if ceiling <= pc:
+            return pc, pf, 0, None
+        if (pf <= 0.0 and frac > 0.0) or (pf > 0.0 and frac >= float(cfg.slow_progress_pressure_trial_min_ratio) * pf):
+            return ceiling, frac, 0, None
+        fails = int(under) + 1
+        if fails >= max(1, int(cfg.slow_progress_pressure_trial_patience)):
+            return pc, pf, 0, ceiling
+        return pc, pf, fails, None
+
+    def _detail_conflict_nets(self, edge_nets):
+        return set(edge_nets) | set(self.path_node_scores) | set(self._find_via_pool_offenders()) | \
+            set(self.barrel_conflict_nets)
+
+    def _detail_pass(self, tasks, initial_overuse, pres_max_now):
+        """``_detail_pass`` (:7593-7788)."""
+        cfg = self.config
+        best_state = self._capture()
+        unrouted0 = sum(1 for n in tasks if not self.net_paths.get(n))
+        best = (unrouted0, int(initial_overuse), int(self.barrel_count))
+        over_map, _, _ = self._over_map()
+        cn = {n for n in self.net_paths if self.net_paths[n]
+              and any(e in over_map for e in self.net_to_edges.get(n, ()))}
+        cn = self._detail_conflict_nets(cn)
+        if not cn:
+            return {'success': False}
+        ctasks = {n: tasks[n] for n in cn if n in tasks}
+        dmax = max(float(cfg.pres_fac_max), float(pres_max_now))
+        pres_fac = dmax * 0.5
+        for _ in range(10):
+            self.ops.update_costs(pres_fac, cfg.hist_cost_weight * 1.5, 0.3, cfg.base_cost_weight, None)
+            self._present_pres_fac = pres_fac
+            hot = self._build_hotset(ctasks, set())
+            if len(hot) > 60:
+                raise RuntimeError("detail-pass hotset above 60 nets depends on Python set order")
+            if not hot:
+                hot = cn
+            sub = {k: v for k, v in ctasks.items() if k in hot}
+            old = self.stagnation_counter
+            self.stagnation_counter += 3
+            self._route_all(sub, tasks)
+            self.stagnation_counter = old
+            over_sum, _ = self._compute_overuse()
+            bc = self._detect_barrels()
+            self.barrel_count = bc
+            pno, _ = self._path_node_overuse()
+            unrouted = {n for n in tasks if not self.net_paths.get(n)}
+            sc = (len(unrouted), int(over_sum) + int(pno), int(bc))
+            if sc < best:
+                best, best_state = sc, self._capture()
+            cn = self._detail_conflict_nets(cn)
+            ctasks.update({n: tasks[n] for n in cn if n in tasks})
+            if over_sum + pno == 0:
+                if unrouted:
+                    cn = unrouted
+                    ctasks.update({n: tasks[n] for n in unrouted})
+                    continue
+                if bc:
+                    continue
+                return {'success': True, 'converged': True, 'paths': self.net_paths}
+            if self.trace is not None:
+                self.trace.append(self._capture())
+            self.ops.update_history(cfg.hist_gain * 2.0, cap_mult=15.0, decay=0.98, use_cap=True,
+                                    use_raw_present=False)
+            pres_fac = min(pres_fac * 1.5, dmax)
+        self._restore(best_state)
+        return {'success': False, 'overuse_sum': best[1]}
+
+
+# the reference exports the same class under this name (:11661)
+UnifiedPathFinder = PathFinderRouter

@@ -1,0 +1,86 @@
+"""End-to-end parity of the GPU router with the CPU oracle loop and with the
+reference's own recorded routing runs (every path of every iteration)."""
+import hashlib
+import json
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+from oracle.lattice import LatticeSpec
+from oracle.loop import Config, OracleRouter
+
+G = os.path.join(os.path.dirname(__file__), "golden")
+META = json.load(open(os.path.join(G, "golden.json")))
+
+
+def board_bounds(nx, ny, pitch=0.4):
+    sx = (nx - 1) * pitch - 6.0 + 1e-6
+    sy = (ny - 1) * pitch - 6.0 + 1e-6
+    return (7.0, 7.0, 10.0 + sx + 3.0, 10.0 + sy + 3.0)
+
+
+def flat(paths):
+    out = []
+    for name in sorted(paths, key=lambda s: int(s[1:])):
+        out.append(len(paths[name]))
+        out.extend(paths[name])
+    return np.asarray(out, dtype=np.int64)
+
+
+def gpu_router(nx, ny, nz, iters):
+    from orthoroute_gb300 import Lattice
+    from orthoroute_gb300.router import PathFinderConfig, PathFinderRouter
+    R = PathFinderRouter(PathFinderConfig(max_iterations=iters))
+    R.initialize_lattice(Lattice(nx, ny, nz), board_bounds(nx, ny))
+    return R
+
+
+@pytest.mark.parametrize("tag", ["r0", "r1"])
+def test_gpu_router_matches_reference_runs(tag):
+    m = META[tag]
+    z = np.load(os.path.join(G, "runs.npz"))
+    reqs = [(f"N{int(r[0])}", int(r[1]), int(r[2])) for r in z[f"{tag}_reqs"]]
+    R = gpu_router(m["nx"], m["ny"], m["nz"], m["iters"])
+    R.trace = []
+    res = R.route_multiple_nets(reqs)
+    n_ref = sum(1 for k in z.files if k.startswith(f"{tag}_it"))
+    assert len(R.trace) == n_ref
+    for j, tr in enumerate(R.trace):
+        np.testing.assert_array_equal(flat(tr), z[f"{tag}_it{j}_paths"], err_msg=f"{tag} record {j}")
+    for a, b in zip(res["iteration_metrics"], m["metrics"]):
+        assert {k: a[k] for k in b} == b
+    assert hashlib.sha256(flat(R.net_paths).tobytes()).hexdigest() == m["final_paths_sha"]
+
+
+def seeded_nets(nx, ny, n, seed, dmin=5, dmax=80):
+    rng = np.random.default_rng(seed)
+    out = []
+    while len(out) < n:
+        x0, x1 = rng.integers(0, nx, size=2)
+        y0, y1 = rng.integers(0, ny, size=2)
+        d = abs(int(x1) - int(x0)) + abs(int(y1) - int(y0))
+        if dmin <= d <= dmax:
+            out.append((f"N{len(out)}", int(y0) * nx + int(x0), int(y1) * nx + int(x1)))
+    return out
+
+
+@pytest.mark.parametrize("dims,n_nets,iters,seed", [((40, 36, 6), 60, 8, 7), ((48, 40, 8), 90, 10, 11)])
+def test_gpu_router_matches_oracle_loop(dims, n_nets, iters, seed):
+    nx, ny, nz = dims
+    reqs = seeded_nets(nx, ny, n_nets, seed)
+    R = gpu_router(nx, ny, nz, iters)
+    R.trace = []
+    res = R.route_multiple_nets(reqs)
+    O = OracleRouter(LatticeSpec(nx, ny, nz), board_bounds(nx, ny), Config(max_iterations=iters))
+    O.trace = []
+    ores = O.route({n: (s, d) for n, s, d in reqs})
+    assert len(R.trace) == len(O.trace)
+    for j, (a, b) in enumerate(zip(R.trace, O.trace)):
+        np.testing.assert_array_equal(flat(a), flat(b), err_msg=f"record {j}")
+    assert bool(res["success"]) == bool(ores["success"])
+    for k in ("barrel_conflicts", "overuse_sum", "failed_nets"):
+        if k in ores and k in res:
+            assert res[k] == ores[k], k

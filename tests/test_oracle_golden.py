@@ -147,3 +147,17 @@ def test_sssp_net_trace_matches_reference():
         # The recorded ROI is what the oracle's BFS extracts too.
         roi2, _ = extract_roi(g.indptr, g.indices, N, g.nx, g.plane, s, d)
         np.testing.assert_array_equal(roi2, roi)
+
+
+@pytest.mark.parametrize("i", range(10))
+def test_c_heap_dijkstra_matches_reference(roi_lattice, i):
+    """The C restatement used by the CPU baseline gives the same paths."""
+    from oracle.dijkstra import find_path_roi_c
+    g = roi_lattice
+    z = np.load(os.path.join(G, "sssp.npz"))
+    s, d, costs, roi, g2r, pen = _sssp_inputs(g, i)
+    st_py, st_c = {}, {}
+    p1 = find_path_roi(g.indptr, g.indices, s, d, costs, roi, g2r, node_penalty=pen, stats=st_py)
+    p2 = find_path_roi_c(g.indptr, g.indices, s, d, costs, roi, g2r, node_penalty=pen, stats=st_c)
+    np.testing.assert_array_equal(np.asarray(p2 or [], dtype=np.int32), z[f"s{i}_path"])
+    assert p1 == p2 and st_py == st_c

@@ -56,3 +56,15 @@ def test_loop_matches_reference_run(tag):
             assert res[k] == ref[k], k
     got_sha = hashlib.sha256(flat(R.net_paths).tobytes()).hexdigest()
     assert got_sha == m["final_paths_sha"]
+
+
+@pytest.mark.parametrize("tag", ["r0", "r1"])
+def test_fast_loop_matches_reference_run(tag):
+    """The loop with the C heap Dijkstra (CPU baseline) is the same restatement."""
+    m = META[tag]
+    z = np.load(os.path.join(G, "runs.npz"))
+    tasks = {f"N{int(r[0])}": (int(r[1]), int(r[2])) for r in z[f"{tag}_reqs"]}
+    R = OracleRouter(LatticeSpec(m["nx"], m["ny"], m["nz"]), board_bounds(m["nx"], m["ny"]),
+                     Config(max_iterations=m["iters"]), fast=True)
+    R.route(tasks)
+    assert hashlib.sha256(flat(R.net_paths).tobytes()).hexdigest() == m["final_paths_sha"]
