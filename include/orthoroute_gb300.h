@@ -102,6 +102,29 @@ int ogr_history_update(int64_t num_edges, float* history, const float* present,
                        const float* base_costs, float gain, float cap_mult,
                        float decay, int32_t use_raw_present, void* stream);
 
+/* ------------------------------------------------------------------ A5 ---
+ * Via pools: penalties (_apply_via_pooling_penalties, CPU branch,
+ * unified_pathfinder.py:5884-5980) and the hard block of saturated columns /
+ * segments (_block_via_edges_with_collisions, :6094-6161) applied to every
+ * via arc of total_cost.  Pools are x-major [nx][ny] and [nx][ny][nz-2];
+ * discount[z_lo*nz+z_hi] (double, may be NULL) is the leave-hot-layer factor.
+ */
+int ogr_via_pools_apply(int64_t num_edges, int32_t nx, int32_t ny, int32_t nz,
+                        const int32_t* edge_src, const int32_t* indices,
+                        const uint8_t* edge_kind, const float* col_pres,
+                        const float* seg_prefix, const int16_t* col_use,
+                        const int16_t* col_cap, const int16_t* seg_use,
+                        const int8_t* seg_cap, const double* discount, float col_weight,
+                        float seg_weight, float pres_fac, int32_t apply_penalty,
+                        int32_t apply_block, float* total_cost, void* stream);
+
+/* Compact the arcs with present > capacity (any order) into out_idx/out_val
+ * (max(0,present-cap)); *count (device) receives the total, which may exceed
+ * out_cap (then only out_cap entries are written). */
+int ogr_overused_arcs(int64_t num_edges, const float* present, const float* capacity,
+                      int32_t* out_idx, float* out_val, int32_t out_cap, uint32_t* count,
+                      void* stream);
+
 /* ------------------------------------------------------------------ A9 ---
  * Tallies (compute_overuse :1137-1190, _compute_path_node_overuse
  * :10718-10726, _compute_layer_bias's bincount :8473-8500).
@@ -193,6 +216,21 @@ int ogr_path_apply(const ogr_graph* g, const ogr_state* st, const int32_t* path,
 int ogr_extract_roi(const ogr_graph* g, const ogr_net_args* net, void* workspace,
                     size_t workspace_bytes, int32_t* roi_out, int32_t roi_cap,
                     int32_t* roi_len_out, void* stream);
+
+/* Allocation-free variant of ogr_find_path.  It has no counterpart in the
+ * reference: it exists for callers that cannot allocate device memory for a
+ * workspace (a plugin inside an application that owns the device allocator,
+ * or a serving process whose memory budget is fixed at start-up).  Its
+ * scratch is a fixed array inside the library (about 73 bytes per node for
+ * OGR_NOALLOC_MAX_NODES nodes, 19 MB, resident on each GPU that loads the library
+ * until exit), so lattices above OGR_NOALLOC_MAX_NODES nodes are refused with
+ * OGR_ERR_CAPACITY.  The first call on a device looks up that array's device
+ * address; make it before any stream capture.  Calls share the array: do not
+ * let two calls overlap on the GPU.  Synchronises like ogr_find_path. */
+#define OGR_NOALLOC_MAX_NODES 262144
+int ogr_find_path_noalloc(const ogr_graph* g, const ogr_state* st, const ogr_net_args* net,
+                          int32_t* path_out, int32_t path_cap, int32_t* path_len_out,
+                          int64_t* stats, void* stream);
 
 #ifdef __cplusplus
 }

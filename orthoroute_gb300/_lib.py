@@ -13,6 +13,8 @@ from . import _build
 
 OGR_OK = 0
 OGR_NO_PATH = 1
+OGR_ERR_CAPACITY = -3
+OGR_NOALLOC_MAX_NODES = 262144
 ERRORS = {-1: "bad argument", -2: "CUDA error", -3: "buffer capacity exceeded",
           -4: "device loop iteration limit reached", -5: "exactness precondition violated"}
 
@@ -21,6 +23,7 @@ EXPORTED = [
     "ogr_costs_update", "ogr_live_begin", "ogr_present_ema", "ogr_history_update",
     "ogr_tally", "ogr_route_workspace_bytes", "ogr_route_workspace_init",
     "ogr_find_path", "ogr_path_apply", "ogr_extract_roi", "ogr_via_pools_apply", "ogr_overused_arcs",
+    "ogr_find_path_noalloc",
 ]
 
 P = C.c_void_p
@@ -95,6 +98,8 @@ def load(build_if_missing: bool = True):
         "ogr_extract_roi": [C.POINTER(Graph), C.POINTER(NetArgs), P, C.c_size_t, P, I32, C.POINTER(I32), P],
         "ogr_via_pools_apply": [I64, I32, I32, I32, P, P, P, P, P, P, P, P, P, P, F32, F32, F32, I32, I32, P, P],
         "ogr_overused_arcs": [I64, P, P, P, P, I32, P, P],
+        "ogr_find_path_noalloc": [C.POINTER(Graph), C.POINTER(State), C.POINTER(NetArgs), P, I32,
+                                  C.POINTER(I32), P, P],
     }
     for name, args in sig.items():
         fn = getattr(lib, name)

@@ -678,3 +678,69 @@ extern "C" int ogr_path_apply(const ogr_graph* g, const ogr_state* st, const int
   OGR_LAUNCH_CHECK();
   return OGR_OK;
 }
+
+// ---- allocation-free search ----------------------------------------------------
+// Some hosts cannot hand this library a workspace: a plugin loaded into an
+// application that owns the device allocator, or a serving process that
+// reserves its whole memory budget at start-up and forbids allocations on the
+// request path.  ogr_find_path_noalloc runs the same search as ogr_find_path
+// with its scratch in a fixed device array that lives in this library's image
+// (resident on every GPU that loads the library until the process exits).
+//
+// Limits and rules:
+//  - at most OGR_NOALLOC_MAX_NODES lattice nodes; larger graphs are rejected
+//    with OGR_ERR_CAPACITY before anything is launched;
+//  - the first call on a device looks up the array's device address for that
+//    device (cudaGetSymbolAddress); make that first call before any stream
+//    capture;
+//  - all calls share the one array: each call re-initialises the parts the
+//    search needs cleared, and calls that overlap on the GPU (another stream,
+//    another host thread) race on it — serialise them.
+namespace {
+
+constexpr size_t noalloc_round(size_t v) { return (v + 255) & ~(size_t)255; }
+
+constexpr size_t noalloc_ws_bytes() {
+  // The layout of ws_layout() for OGR_NOALLOC_MAX_NODES nodes: 16 int32 /
+  // float arrays, one double array, one byte array, the 64-byte result block,
+  // each rounded up to 256 bytes (about 19 MB).
+  return 16 * noalloc_round((size_t)OGR_NOALLOC_MAX_NODES * 4) + noalloc_round((size_t)OGR_NOALLOC_MAX_NODES * 8) +
+         noalloc_round((size_t)OGR_NOALLOC_MAX_NODES) + noalloc_round(64);
+}
+
+static __device__ __align__(256) unsigned char g_noalloc_ws[noalloc_ws_bytes()];
+
+constexpr int kMaxDevices = 64;
+void* g_noalloc_ptr[kMaxDevices] = {};
+
+}  // namespace
+
+extern "C" int ogr_find_path_noalloc(const ogr_graph* g, const ogr_state* st, const ogr_net_args* net,
+                                     int32_t* path_out, int32_t path_cap, int32_t* path_len_out, int64_t* stats,
+                                     void* stream) {
+  if (!g || !st || !net || !path_out || !path_len_out) return OGR_ERR_ARG;
+  if (g->num_nodes < 1 || g->num_nodes > OGR_NOALLOC_MAX_NODES) return OGR_ERR_CAPACITY;
+  if (net->src < 0 || net->dst < 0 || net->src >= g->num_nodes || net->dst >= g->num_nodes) return OGR_ERR_ARG;
+  int dev = 0;
+  OGR_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kMaxDevices) return OGR_ERR_ARG;
+  if (g_noalloc_ptr[dev] == nullptr) {
+    void* p = nullptr;
+    OGR_CUDA_TRY(cudaGetSymbolAddress(&p, g_noalloc_ws));
+    g_noalloc_ptr[dev] = p;
+  }
+  const size_t need = ws_layout(g->num_nodes, nullptr, nullptr);
+  if (need > noalloc_ws_bytes()) return OGR_ERR_CAPACITY;
+  Ws w;
+  ws_layout(g->num_nodes, (char*)g_noalloc_ptr[dev], &w);
+  cudaStream_t s = ogr_stream(stream);
+  // The array keeps whatever the previous call left: clear seen[] / g2r[].
+  ws_init_kernel<<<ogr_blocks(g->num_nodes, 256), 256, 0, s>>>(w, g->num_nodes);
+  find_path_kernel<<<1, kThreads, 0, s>>>(*g, *st, *net, w, path_out, path_cap, stats);
+  OGR_LAUNCH_CHECK();
+  int64_t res[2];
+  OGR_CUDA_TRY(cudaMemcpyAsync(res, w.result, sizeof(res), cudaMemcpyDeviceToHost, s));
+  OGR_CUDA_TRY(cudaStreamSynchronize(s));
+  *path_len_out = (res[0] == OGR_OK) ? (int32_t)res[1] : 0;
+  return (int)res[0];
+}
