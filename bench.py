@@ -137,7 +137,7 @@ def run_ours(args, cfg, rank, world):
         router.initialize_state()
         return router.route_multiple_nets(reqs)
 
-    router = PathFinderRouter(PathFinderConfig(max_iterations=cfg["iters"]))
+    router = PathFinderRouter(PathFinderConfig(max_iterations=cfg["iters"]), mode=args.mode)
     router.initialize_lattice(Lattice(nx, ny, nz), bounds)
     for _ in range(args.warmup):
         job(router)
@@ -166,13 +166,25 @@ def run_ours(args, cfg, rank, world):
     for _ in range(max(1, min(args.steps, 2))):
         torch.cuda.synchronize()
         t1 = time.perf_counter()
-        r2 = PathFinderRouter(PathFinderConfig(max_iterations=cfg["iters"]))
+        r2 = PathFinderRouter(PathFinderConfig(max_iterations=cfg["iters"]), mode=args.mode)
         r2.initialize_lattice(Lattice(nx, ny, nz), bounds)
         res2 = r2.route_multiple_nets(reqs)
         _ = {k: list(v) for k, v in res2["paths"].items()}
         torch.cuda.synchronize()
         e2e_t.append(time.perf_counter() - t1)
         del r2
+    plain = None
+    if args.mode == "persistent" and args.compare_plain:
+        rp = PathFinderRouter(PathFinderConfig(max_iterations=cfg["iters"]), mode="plain")
+        rp.initialize_lattice(Lattice(nx, ny, nz), bounds)
+        rp.initialize_state()
+        torch.cuda.synchronize()
+        t2 = time.perf_counter()
+        resp = rp.route_multiple_nets(reqs)
+        torch.cuda.synchronize()
+        plain = time.perf_counter() - t2
+        same = {k: list(v) for k, v in resp["paths"].items()} == {k: list(v) for k, v in results[-1]["paths"].items()}
+        del rp
     clocks = sampler.stop()
     ms = max(dev_ms, wall * 1e3) / args.steps
     if dist:
@@ -211,7 +223,11 @@ def run_ours(args, cfg, rank, world):
                 "d2h_bytes_per_step": prof["d2h_bytes"] // max(1, args.steps)},
         "gpu_launches": prof["launches"] // max(1, args.steps),
         "clocks": clocks,
+        "mode": args.mode,
     }
+    if plain is not None:
+        line["plain_one_net_per_launch_s_per_job"] = round(plain, 4)
+        line["plain_identical_paths"] = bool(same)
     return line
 
 
@@ -262,6 +278,9 @@ def main():
     ap.add_argument("--config", default="c0", choices=sorted(CONFIGS))
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--mode", default="persistent", choices=["persistent", "plain"])
+    ap.add_argument("--compare-plain", action="store_true", default=True)
+    ap.add_argument("--no-compare-plain", dest="compare_plain", action="store_false")
     args = ap.parse_args()
     cfg = CONFIGS[args.config]
     rank = int(os.environ.get("RANK", "0"))

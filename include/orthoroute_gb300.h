@@ -217,12 +217,84 @@ int ogr_extract_roi(const ogr_graph* g, const ogr_net_args* net, void* workspace
                     size_t workspace_bytes, int32_t* roi_out, int32_t roi_cap,
                     int32_t* roi_len_out, void* stream);
 
+/* --------------------------------------------------------------- A8/A10 ---
+ * One routing pass in one launch: for each net of `order`, in order, the
+ * sequence of _route_all (unified_pathfinder.py:7949-8449): rip up its stored
+ * path, search its ROI (or the whole graph), retry once with the larger
+ * fallback ROI while the pass has fallbacks left (< 5 per iteration,
+ * :8337-8370), commit the new path.  Paths live in a device store of
+ * num_nets slots of slot_cap nodes; store_arcs receives each committed path's
+ * arcs (forward then reverse).  net_status[k] = 1 if the k-th net failed,
+ * | 2 if it used a fallback.  Synchronises; returns OGR_OK or an error. */
+typedef struct {
+  int32_t num_nets;
+  int32_t slot_cap;
+  int32_t* store_len;          /* [num_nets] nodes of the current path (0 = none) */
+  int32_t* store_path;         /* [num_nets * slot_cap]                           */
+  int32_t* store_arcs;         /* [num_nets * 2 * slot_cap]                       */
+  const int32_t* net_src;
+  const int32_t* net_dst;
+  const int32_t* net_id;       /* ownership id of each net                        */
+  const int32_t* net_full;     /* 1: full-graph search (Manhattan >= 125)         */
+  const int32_t* net_depth;    /* [2*num_nets] BFS depth: normal, fallback        */
+  const int32_t* net_halo;     /* [2*num_nets] BFS halo: normal, fallback         */
+} ogr_net_table;
+
+typedef struct {
+  const int32_t* order;
+  int32_t count;
+  int32_t fallback_quota;
+  int32_t max_roi_nodes;
+  double bfs_stop_count;
+  float owner_weight;
+  float path_weight;
+  float history_weight;
+  int32_t penalty_enabled;
+  float pres_fac;              /* float32(pres_fac) for the live refresh          */
+  int32_t live;
+  int32_t* net_status;         /* [count]                                         */
+  int64_t* stats;              /* [4] accumulated search statistics               */
+} ogr_pass_args;
+
+/* Optional batched ROI extraction for a pass: before the sequential part,
+ * `slots` CTAs extract the ROIs of all ROI nets of `order` in parallel (the
+ * BFS reads no costs), each into roi_pool[n*roi_cap] (roi_cap >= the pass's
+ * max_roi_nodes), roi_len[n] = size or -1 (queue overflow: that net's ROI
+ * is then extracted inline).  bfs_ws holds `slots` slots of slot_bytes
+ * (ogr_bfs_workspace_bytes / ogr_bfs_workspace_init); next is a device int. */
+typedef struct {
+  int32_t slots;
+  size_t slot_bytes;
+  int64_t qcap;
+  void* bfs_ws;
+  int32_t* roi_pool;
+  int32_t* roi_len;
+  int32_t roi_cap;
+  int32_t* next;
+} ogr_roi_batch;
+
+size_t ogr_bfs_workspace_bytes(int32_t num_nodes, int64_t qcap, int32_t slots);
+int ogr_bfs_workspace_init(void* workspace, int32_t num_nodes, int64_t qcap, int32_t slots,
+                           void* stream);
+
+/* rb may be NULL (every ROI is extracted inline, in order). */
+int ogr_route_pass(const ogr_graph* g, const ogr_state* st, const ogr_net_table* t,
+                   const ogr_pass_args* pa, const ogr_roi_batch* rb, void* workspace,
+                   size_t workspace_bytes, int32_t* status_out, void* stream);
+
+/* Tracing: cumulative per-stage cycle counters of all searches on the
+ * current device since the last reset (host int64[16]: BFS, compaction,
+ * search init, queueing, recompute, frontier min, settle, statistics and
+ * backtrace, cleanup; then searches, settle phases, BFS waves, ROI nodes,
+ * recomputed nodes).  Synchronous. */
+int ogr_search_profile(int64_t* out16, int32_t reset);
+
 /* Allocation-free variant of ogr_find_path.  It has no counterpart in the
  * reference: it exists for callers that cannot allocate device memory for a
  * workspace (a plugin inside an application that owns the device allocator,
  * or a serving process whose memory budget is fixed at start-up).  Its
- * scratch is a fixed array inside the library (about 73 bytes per node for
- * OGR_NOALLOC_MAX_NODES nodes, 19 MB, resident on each GPU that loads the library
+ * scratch is a fixed array inside the library (36 MB: about 76 bytes per
+ * node for OGR_NOALLOC_MAX_NODES nodes plus a 16 MB local adjacency, resident on each GPU that loads the library
  * until exit), so lattices above OGR_NOALLOC_MAX_NODES nodes are refused with
  * OGR_ERR_CAPACITY.  The first call on a device looks up that array's device
  * address; make it before any stream capture.  Calls share the array: do not

@@ -23,7 +23,8 @@ EXPORTED = [
     "ogr_costs_update", "ogr_live_begin", "ogr_present_ema", "ogr_history_update",
     "ogr_tally", "ogr_route_workspace_bytes", "ogr_route_workspace_init",
     "ogr_find_path", "ogr_path_apply", "ogr_extract_roi", "ogr_via_pools_apply", "ogr_overused_arcs",
-    "ogr_find_path_noalloc",
+    "ogr_find_path_noalloc", "ogr_route_pass", "ogr_search_profile", "ogr_bfs_workspace_bytes",
+    "ogr_bfs_workspace_init",
 ]
 
 P = C.c_void_p
@@ -63,6 +64,23 @@ class NetArgs(C.Structure):
                 ("penalty_enabled", I32)]
 
 
+class NetTable(C.Structure):
+    _fields_ = [("num_nets", I32), ("slot_cap", I32), ("store_len", P), ("store_path", P), ("store_arcs", P),
+                ("net_src", P), ("net_dst", P), ("net_id", P), ("net_full", P), ("net_depth", P), ("net_halo", P)]
+
+
+class PassArgs(C.Structure):
+    _fields_ = [("order", P), ("count", I32), ("fallback_quota", I32), ("max_roi_nodes", I32),
+                ("bfs_stop_count", C.c_double), ("owner_weight", F32), ("path_weight", F32),
+                ("history_weight", F32), ("penalty_enabled", I32), ("pres_fac", F32), ("live", I32),
+                ("net_status", P), ("stats", P)]
+
+
+class RoiBatch(C.Structure):
+    _fields_ = [("slots", I32), ("slot_bytes", C.c_size_t), ("qcap", I64), ("bfs_ws", P), ("roi_pool", P),
+                ("roi_len", P), ("roi_cap", I32), ("next", P)]
+
+
 _LIB = None
 
 
@@ -100,6 +118,11 @@ def load(build_if_missing: bool = True):
         "ogr_overused_arcs": [I64, P, P, P, P, I32, P, P],
         "ogr_find_path_noalloc": [C.POINTER(Graph), C.POINTER(State), C.POINTER(NetArgs), P, I32,
                                   C.POINTER(I32), P, P],
+        "ogr_search_profile": [P, I32],
+        "ogr_route_pass": [C.POINTER(Graph), C.POINTER(State), C.POINTER(NetTable), C.POINTER(PassArgs),
+                           C.POINTER(RoiBatch), P, C.c_size_t, C.POINTER(I32), P],
+        "ogr_bfs_workspace_bytes": [I32, I64, I32],
+        "ogr_bfs_workspace_init": [P, I32, I64, I32, P],
     }
     for name, args in sig.items():
         fn = getattr(lib, name)

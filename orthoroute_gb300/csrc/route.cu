@@ -1,6 +1,5 @@
 // A6–A8: per-net ROI extraction, exact ROI shortest path, backtrace, and the
-// commit / rip-up scatter.  One CTA (1024 threads) owns one net's search; the
-// batched entry points run one CTA per independent net.
+// commit / rip-up scatter.  One CTA (1024 threads) owns one net's search.
 //
 // ROI (extract_roi_bfs, unified_pathfinder.py:2257-2384): level-synchronous
 // bidirectional BFS.  Within one wave step the reference's marks are a set
@@ -8,7 +7,9 @@
 // "met"), so claiming nodes with atomicCAS yields the same seen[] array,
 // meeting depth and early stop.  The ROI is then compacted in ascending
 // global id order (np.where) by scanning the BFS bounding box, and truncated
-// to max_roi_nodes with the reference's must-keep swap.
+// to max_roi_nodes with the reference's must-keep swap.  The BFS does not read
+// costs, so a routing pass extracts the ROIs of all its nets in parallel on
+// many SMs before the sequential part starts (roi_batch_kernel).
 //
 // Search (SimpleDijkstra.find_path_roi, :2451-2548): the reference pops
 // (label, roi_idx) from a heap of FP64 labels, and accepts a relaxation iff
@@ -23,91 +24,119 @@
 // and nodes whose label equals T are final as in Dijkstra.  Tentative states
 // are recomputed by pulling from all settled in-neighbours, which makes the
 // result independent of thread scheduling and bit-identical to the heap.
+//
+// Latency: before the phases, each search gathers an ROI-local adjacency
+// (neighbour's ROI index and the in-arc cost, 32 slots per node, one 128-byte
+// row) so a phase touches two dependent loads per arc instead of six; a
+// 16-lane group handles one node's arcs in parallel; node state is packed in
+// one 32-byte sector; the per-group key reduction uses shuffles.
+//
+// ogr_route_pass runs the reference's per-net sequence (_route_all,
+// :7949-8449: rip-up, ROI search, one larger-ROI retry while the pass has
+// fallbacks left, commit) for a whole ordered list of nets in one launch,
+// with every net's current path kept in a device-resident store.
 #include "common.cuh"
 
 namespace {
 
 constexpr int kThreads = 1024;
 constexpr int kWarps = kThreads / 32;
-constexpr uint8_t ST_NONE = 0, ST_FRONT = 1, ST_DONE = 2;
+constexpr int kSub = 16;                       // lanes per node
+constexpr int kGroups = kThreads / kSub;       // nodes in flight per CTA
+constexpr int32_t ST_NONE = 0, ST_FRONT = 1, ST_DONE = 2;
+constexpr int kMaxViaNodes = 4096;
+constexpr int kDMax = 32;                      // arcs per node the local adjacency holds
+constexpr int kAdjCap = 65536;                 // ROI nodes the local adjacency holds
+
+struct __align__(32) NodeSt {
+  double lab;      // FP64 label (tentative until settled)
+  float m32;       // float32 key of the label
+  float pen;       // node penalty (fixed once reached)
+  float cin;       // cheapest in-arc cost from an unsettled ROI neighbour
+  int32_t par;     // ROI index of the winning relaxer
+  int32_t st;      // ST_NONE / ST_FRONT / ST_DONE
+  int32_t stamp;   // phase in which the node was last queued for recompute
+};
+static_assert(sizeof(NodeSt) == 32, "NodeSt must fill one 32-byte sector");
 
 struct Ws {
   int32_t* seen;
   int32_t* g2r;
   int32_t* q[4];
   int32_t* roi;
-  double* lab;
-  float* m32;
-  int32_t* par;
-  float* pen;
-  float* cin;
+  NodeSt* node;
   int32_t* fr[2];
   int32_t* dl;
-  int32_t* dstamp;
   int32_t* blist;
-  uint8_t* st;
-  int64_t* result;  // [0] status, [1] path len, [2..5] stats
+  int32_t* adj;      // [kAdjCap][kDMax] neighbour ROI index or -1
+  float* acost;      // [kAdjCap][kDMax] cost of the arc neighbour -> node
+  int32_t* deg;      // [kAdjCap] arcs of the node
+  int64_t* result;   // [0] status, [1] path len
+  int64_t qcap;
 };
 
-__host__ __device__ inline size_t align_up(size_t v) { return (v + 255) & ~(size_t)255; }
+__host__ __device__ constexpr size_t round256(size_t v) { return (v + 255) & ~(size_t)255; }
+__host__ __device__ constexpr size_t min_sz(size_t a, size_t b) { return a < b ? a : b; }
+
+// Bytes of one search slot for n nodes.
+__host__ __device__ constexpr size_t ws_bytes_for(size_t n) {
+  return 10 * round256(4 * n) + round256(32 * n) + 2 * round256(4 * min_sz(n, kAdjCap) * kDMax) +
+         round256(4 * min_sz(n, kAdjCap)) + round256(64);
+}
 
 __host__ inline size_t ws_layout(int32_t N, char* base, Ws* w) {
   size_t off = 0;
   auto take = [&](size_t bytes) -> char* {
     char* p = base ? base + off : nullptr;
-    off = align_up(off + bytes);
+    off += round256(bytes);
     return p;
   };
   const size_t n = (size_t)N;
+  const size_t a = min_sz(n, kAdjCap);
   Ws t{};
   t.seen = (int32_t*)take(4 * n);
   t.g2r = (int32_t*)take(4 * n);
   for (int i = 0; i < 4; ++i) t.q[i] = (int32_t*)take(4 * n);
   t.roi = (int32_t*)take(4 * n);
-  t.lab = (double*)take(8 * n);
-  t.m32 = (float*)take(4 * n);
-  t.par = (int32_t*)take(4 * n);
-  t.pen = (float*)take(4 * n);
-  t.cin = (float*)take(4 * n);
   t.fr[0] = (int32_t*)take(4 * n);
   t.fr[1] = (int32_t*)take(4 * n);
   t.dl = (int32_t*)take(4 * n);
-  t.dstamp = (int32_t*)take(4 * n);
-  t.blist = (int32_t*)take(4 * n);
-  t.st = (uint8_t*)take(n);
-  t.result = (int64_t*)take(8 * 8);
+  t.node = (NodeSt*)take(32 * n);
+  t.adj = (int32_t*)take(4 * a * kDMax);
+  t.acost = (float*)take(4 * a * kDMax);
+  t.deg = (int32_t*)take(4 * a);
+  t.blist = t.q[0];  // the BFS queues are free while the search runs
+  t.result = (int64_t*)take(64);
+  t.qcap = (int64_t)n;
   if (w) *w = t;
   return off;
 }
 
-// ---- block primitives ------------------------------------------------------
-__device__ __forceinline__ int block_excl_scan(int v, int* s_warp, int* total) {
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  int x = v;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    int y = __shfl_up_sync(0xffffffffu, x, o);
-    if (lane >= o) x += y;
-  }
-  if (lane == 31) s_warp[wid] = x;
-  __syncthreads();
-  if (wid == 0) {
-    int w = (lane < kWarps) ? s_warp[lane] : 0;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      int y = __shfl_up_sync(0xffffffffu, w, o);
-      if (lane >= o) w += y;
-    }
-    if (lane < kWarps) s_warp[lane] = w;  // inclusive
-    if (lane == kWarps - 1) *total = w;
-  }
-  __syncthreads();
-  const int before = (wid == 0) ? 0 : s_warp[wid - 1];
-  const int res = before + x - v;
-  __syncthreads();
-  return res;
+// A BFS-only slot for the batched ROI extraction: seen[N] + 4 queues.
+struct BfsSlot {
+  int32_t* seen;
+  int32_t* q[4];
+  int64_t qcap;
+};
+
+__host__ inline size_t bfs_slot_bytes(int32_t N, int64_t qcap) {
+  return round256(4 * (size_t)N) + 4 * round256(4 * (size_t)qcap);
 }
 
+__host__ __device__ inline BfsSlot bfs_slot_at(char* base, int32_t N, int64_t qcap) {
+  BfsSlot s;
+  size_t off = 0;
+  s.seen = (int32_t*)(base + off);
+  off += round256(4 * (size_t)N);
+  for (int i = 0; i < 4; ++i) {
+    s.q[i] = (int32_t*)(base + off);
+    off += round256(4 * (size_t)qcap);
+  }
+  s.qcap = qcap;
+  return s;
+}
+
+// ---- block primitives ------------------------------------------------------
 __device__ __forceinline__ unsigned long long block_min_u64(unsigned long long v, unsigned long long* s) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
@@ -132,19 +161,6 @@ __device__ __forceinline__ unsigned long long block_min_u64(unsigned long long v
   return r;
 }
 
-struct Key {  // lexicographic (float32 alt, L(u), roi idx of u)
-  float a32;
-  double lu;
-  int32_t u;
-  double alt;
-};
-
-__device__ __forceinline__ bool key_less(float a32, double lu, int32_t u, const Key& k) {
-  if (a32 != k.a32) return a32 < k.a32;
-  if (lu != k.lu) return lu < k.lu;
-  return u < k.u;
-}
-
 __device__ __forceinline__ float node_penalty(const ogr_state& st, const ogr_net_args& a, int32_t gid) {
   if (!a.penalty_enabled) return 0.0f;
   const int32_t cnt = st.owner_count[gid];
@@ -156,420 +172,551 @@ __device__ __forceinline__ float node_penalty(const ogr_state& st, const ogr_net
   return __fadd_rn(__fadd_rn(f, o), __fmul_rn(st.node_history[gid], a.history_weight));
 }
 
-// ---- the per-net search kernel -----------------------------------------------
+// (a32, lu, u) lexicographic less-than.
+__device__ __forceinline__ bool key_lt(float a1, double l1, int32_t u1, float a2, double l2, int32_t u2) {
+  if (a1 != a2) return a1 < a2;
+  if (l1 != l2) return l1 < l2;
+  return u1 < u2;
+}
+
+// Per-stage cycle counters of the search (a tracing aid, read with
+// ogr_search_profile): [0] BFS waves, [1] ROI compaction, [2] SSSP init and
+// local adjacency, [3] phase queueing, [4] recompute, [5] frontier min,
+// [6] settle, [7] statistics + backtrace, [8] cleanup, [9] searches,
+// [10] phases, [11] BFS waves run, [12] ROI nodes, [13] recomputed nodes,
+// [14] ROIs taken from the batched extraction.
+__device__ unsigned long long g_stage[16];
+
 struct Shared {
-  int s_warp[kWarps];
   unsigned long long s_min[kWarps];
-  int total;
+  int s_cnt[kWarps];
+  int s_off[kWarps];
   int nq[4];
   int seen_count;
   int met;
+  int overflow;
   int bx0, bx1, by0, by1;
+  int pos_src, pos_dst;
   int R;
   int nfront, nnext, ndirty, nb;
   int status;
   int found;
+  int len;
+  int local;
 };
 
-__device__ void search_one(const ogr_graph& g, const ogr_state& st, const ogr_net_args& a, const Ws& w,
-                           int32_t* path_out, int32_t path_cap, bool roi_only, int32_t* roi_out, int32_t roi_cap,
-                           int64_t* stats_out) {
-  __shared__ Shared sh;
-  const int tid = threadIdx.x;
-  const int nx = g.nx, ny = g.ny, nz = g.nz;
-  const int64_t plane = (int64_t)nx * ny;
-  const int32_t src = a.src, dst = a.dst;
-  const bool full = a.full_graph != 0;
-  const int32_t* indptr = g.indptr;
-  const int32_t* indices = g.indices;
-
-  if (tid == 0) {
-    sh.status = OGR_OK;
-    sh.found = 0;
-  }
-  // ------------------------------------------------------------------ ROI
-  if (!full) {
-    if (tid == 0) {
-      w.seen[src] = 1;
-      w.seen[dst] = 2;
-      w.q[0][0] = src;
-      w.q[2][0] = dst;
-      sh.nq[0] = 1;
-      sh.nq[2] = 1;
-      sh.seen_count = (src != dst) ? 2 : 1;
-      const int sy = (int)((src % plane) / nx), sx = (int)((src % plane) % nx);
-      const int dy = (int)((dst % plane) / nx), dx = (int)((dst % plane) % nx);
-      sh.bx0 = min(sx, dx); sh.bx1 = max(sx, dx);
-      sh.by0 = min(sy, dy); sh.by1 = max(sy, dy);
-      sh.met = 0;
+struct StageClock {
+  long long t;
+  __device__ void start() { t = clock64(); }
+  __device__ void mark(int k) {
+    if (threadIdx.x == 0) {
+      const long long now = clock64();
+      atomicAdd(&g_stage[k], (unsigned long long)(now - t));
+      t = now;
     }
-    __syncthreads();
-    int depth = 0, meet = -1;
-    int cur_s = 0, cur_d = 2;
-    while (depth < a.bfs_max_depth && (sh.nq[cur_s] > 0 || sh.nq[cur_d] > 0)) {
-      for (int wave = 0; wave < 2; ++wave) {
-        const int cur = wave == 0 ? cur_s : cur_d;
-        const int nxt = cur ^ 1;
-        const int32_t mark = wave == 0 ? 1 : 2;
-        if (tid == 0) sh.nq[nxt] = 0;
-        __syncthreads();
-        const int n = sh.nq[cur];
-        const int32_t* qc = w.q[cur];
-        int32_t* qn = w.q[nxt];
-        int local_met = 0, local_new = 0;
-        int lx0 = 1 << 30, lx1 = -1, ly0 = 1 << 30, ly1 = -1;
-        for (int i = tid; i < n; i += kThreads) {
-          const int32_t u = qc[i];
-          const int32_t e1 = indptr[u + 1];
-          for (int32_t e = indptr[u]; e < e1; ++e) {
-            if (g.blocked != nullptr && g.blocked[e]) continue;
-            const int32_t v = indices[e];
-            const int32_t old = atomicCAS(&w.seen[v], 0, mark);
-            if (old == 0) {
-              const int pos = atomicAdd(&sh.nq[nxt], 1);
-              qn[pos] = v;
-              ++local_new;
-              const int64_t r = v % plane;
-              const int vy = (int)(r / nx), vx = (int)(r % nx);
-              lx0 = min(lx0, vx); lx1 = max(lx1, vx);
-              ly0 = min(ly0, vy); ly1 = max(ly1, vy);
-            } else if (old != mark) {
-              w.seen[v] = 3;
-              local_met = 1;
-            }
+  }
+};
+
+// ---- ROI extraction ---------------------------------------------------------
+// Bidirectional BFS from src/dst on seen[] (all zero on entry, restored to
+// zero on exit) with queues of qcap entries; writes the ROI (ascending id,
+// truncated with the must-keep swap) into out[0..out_cap) and its size into
+// sh.R.  sh.status = OGR_ERR_CAPACITY when a queue overflowed.
+__device__ void roi_build(Shared& sh, const ogr_graph& g, const ogr_net_args& a, int32_t* seen, int32_t* const* q,
+                          int64_t qcap, int32_t* out, int32_t out_cap, StageClock& clk) {
+  const int tid = threadIdx.x;
+  const int lane = tid & 31, warp = tid >> 5;
+  const int sl = tid & (kSub - 1), grp = tid / kSub;
+  const int nx = g.nx, nz = g.nz;
+  const int32_t plane = nx * g.ny;
+  const int32_t src = a.src, dst = a.dst;
+  const int32_t* __restrict__ indptr = g.indptr;
+  const int32_t* __restrict__ indices = g.indices;
+  if (tid == 0) {
+    seen[src] = 1;
+    seen[dst] = 2;
+    q[0][0] = src;
+    q[2][0] = dst;
+    sh.nq[0] = 1;
+    sh.nq[2] = 1;
+    sh.seen_count = (src != dst) ? 2 : 1;
+    sh.overflow = 0;
+    const int sy = (src % plane) / nx, sx = (src % plane) % nx;
+    const int dy = (dst % plane) / nx, dx = (dst % plane) % nx;
+    sh.bx0 = min(sx, dx); sh.bx1 = max(sx, dx);
+    sh.by0 = min(sy, dy); sh.by1 = max(sy, dy);
+    sh.met = 0;
+    sh.pos_src = -1;
+    sh.pos_dst = -1;
+  }
+  __syncthreads();
+  int depth = 0, meet = -1;
+  int cur_s = 0, cur_d = 2;
+  while (depth < a.bfs_max_depth && (sh.nq[cur_s] > 0 || sh.nq[cur_d] > 0)) {
+    for (int wave = 0; wave < 2; ++wave) {
+      const int cur = wave == 0 ? cur_s : cur_d;
+      const int nxt = cur ^ 1;
+      const int32_t mark = wave == 0 ? 1 : 2;
+      if (tid == 0) sh.nq[nxt] = 0;
+      __syncthreads();
+      const int n = (int)min((int64_t)sh.nq[cur], qcap);
+      const int32_t* qc = q[cur];
+      int32_t* qn = q[nxt];
+      int local_met = 0, local_new = 0, local_ovf = 0;
+      int lx0 = 1 << 30, lx1 = -1, ly0 = 1 << 30, ly1 = -1;
+      for (int i = grp; i < n; i += kGroups) {
+        const int32_t u = qc[i];
+        const int32_t e1 = indptr[u + 1];
+        for (int32_t e = indptr[u] + sl; e < e1; e += kSub) {
+          if (g.blocked != nullptr && g.blocked[e]) continue;
+          const int32_t v = indices[e];
+          const int32_t old = atomicCAS(&seen[v], 0, mark);
+          if (old == 0) {
+            const int pos = atomicAdd(&sh.nq[nxt], 1);
+            if (pos < qcap) qn[pos] = v; else local_ovf = 1;
+            ++local_new;
+            const int32_t r = v % plane;
+            const int vy = r / nx, vx = r % nx;
+            lx0 = min(lx0, vx); lx1 = max(lx1, vx);
+            ly0 = min(ly0, vy); ly1 = max(ly1, vy);
+          } else if (old != mark) {
+            seen[v] = 3;
+            local_met = 1;
           }
         }
+      }
+      local_new = __reduce_add_sync(0xffffffffu, local_new);
+      local_met = __reduce_or_sync(0xffffffffu, local_met);
+      local_ovf = __reduce_or_sync(0xffffffffu, local_ovf);
+      lx0 = __reduce_min_sync(0xffffffffu, lx0);
+      lx1 = __reduce_max_sync(0xffffffffu, lx1);
+      ly0 = __reduce_min_sync(0xffffffffu, ly0);
+      ly1 = __reduce_max_sync(0xffffffffu, ly1);
+      if (lane == 0) {
         if (local_met) sh.met = 1;
+        if (local_ovf) sh.overflow = 1;
         if (local_new) {
           atomicAdd(&sh.seen_count, local_new);
           atomicMin(&sh.bx0, lx0); atomicMax(&sh.bx1, lx1);
           atomicMin(&sh.by0, ly0); atomicMax(&sh.by1, ly1);
         }
-        __syncthreads();
-        if (wave == 0) cur_s = nxt; else cur_d = nxt;
       }
-      ++depth;
-      if (sh.met && meet < 0) meet = depth;
-      if (meet >= 0 && depth >= meet + a.bfs_halo) break;
-      if ((double)sh.seen_count > a.bfs_stop_count) break;
-    }
-    __syncthreads();
-    // Ordered compaction over the bounding box: ascending global id.
-    const int W = sh.bx1 - sh.bx0 + 1, H = sh.by1 - sh.by0 + 1;
-    const int64_t area = (int64_t)W * H;
-    const int64_t V = area * nz;
-    int base = 0;
-    for (int64_t start = 0; start < V; start += kThreads) {
-      const int64_t i = start + tid;
-      int32_t gid = -1;
-      int flag = 0;
-      if (i < V) {
-        const int z = (int)(i / area);
-        const int64_t rem = i - (int64_t)z * area;
-        const int y = sh.by0 + (int)(rem / W);
-        const int x = sh.bx0 + (int)(rem % W);
-        gid = (int32_t)(z * plane + (int64_t)y * nx + x);
-        flag = w.seen[gid] != 0;
-      }
-      const int pos = block_excl_scan(flag, sh.s_warp, &sh.total);
-      if (flag) w.roi[base + pos] = gid;
-      base += sh.total;
       __syncthreads();
+      if (wave == 0) cur_s = nxt; else cur_d = nxt;
     }
-    if (tid == 0) {
-      int R = base;
-      if (R > a.max_roi_nodes) {
-        // Must-keep swap (extract_roi_bfs :2359-2379): positions of src/dst in
-        // ascending order; each one beyond the cut swaps with slot 0 / 1.
-        int kept[2];
-        int nk = 0;
-        for (int pass = 0; pass < 2; ++pass) {
-          const int32_t target = pass == 0 ? min(src, dst) : max(src, dst);
-          if (pass == 1 && src == dst) break;
-          int lo = 0, hi = R - 1, found = -1;
-          while (lo <= hi) {
-            const int mid = (lo + hi) >> 1;
-            const int32_t vmid = w.roi[mid];
-            if (vmid == target) { found = mid; break; }
-            if (vmid < target) lo = mid + 1; else hi = mid - 1;
-          }
-          if (found >= 0) kept[nk++] = found;
-        }
-        for (int k = 0; k < nk; ++k) {
-          if (kept[k] >= a.max_roi_nodes) {
-            const int32_t t = w.roi[kept[k]];
-            w.roi[kept[k]] = w.roi[k];
-            w.roi[k] = t;
-          }
-        }
-        R = a.max_roi_nodes;
-      }
-      sh.R = R;
-    }
-    __syncthreads();
-    for (int r = tid; r < sh.R; r += kThreads) w.g2r[w.roi[r]] = r;
-    __syncthreads();
-  } else {
-    if (tid == 0) sh.R = g.num_nodes;
-    __syncthreads();
+    ++depth;
+    if (tid == 0) atomicAdd(&g_stage[11], 2ull);
+    if (sh.met && meet < 0) meet = depth;
+    if (meet >= 0 && depth >= meet + a.bfs_halo) break;
+    if ((double)sh.seen_count > a.bfs_stop_count) break;
+    if (sh.overflow) break;
   }
-  const int R = sh.R;
-
-  if (roi_only) {
-    if (tid == 0 && R > roi_cap) sh.status = OGR_ERR_CAPACITY;
-    __syncthreads();
-    if (sh.status == OGR_OK)
-      for (int r = tid; r < R; r += kThreads) roi_out[r] = full ? r : w.roi[r];
-    if (tid == 0) w.result[1] = R;
-  } else {
-    // ---------------------------------------------------------------- SSSP
-    const int32_t rs = full ? src : w.g2r[src];
-    const int32_t rd = full ? dst : w.g2r[dst];
-    for (int r = tid; r < R; r += kThreads) {
-      w.st[r] = ST_NONE;
-      w.dstamp[r] = -1;
+  __syncthreads();
+  clk.mark(0);
+  // Ordered compaction over the bounding box (ascending global id): each warp
+  // owns a contiguous segment; count, scan the 32 counts, then write.  Only
+  // positions below out_cap are stored; those of src and dst are recorded.
+  const int W = sh.bx1 - sh.bx0 + 1, H = sh.by1 - sh.by0 + 1;
+  const int32_t area = W * H;
+  const int32_t V = area * nz;
+  const int32_t seg = (((V + kWarps - 1) / kWarps) + 31) & ~31;
+  const int32_t w0 = warp * seg, w1 = min(V, w0 + seg);
+  const int bx0 = sh.bx0, by0 = sh.by0;
+  auto gid_of = [&](int32_t i) -> int32_t {
+    const int z = i / area;
+    const int32_t rem = i - z * area;
+    const int y = by0 + rem / W;
+    const int x = bx0 + rem % W;
+    return z * plane + y * nx + x;
+  };
+  int cnt = 0;
+  for (int32_t b = w0; b < w1; b += 32) {
+    const int32_t i = b + lane;
+    const bool f = i < w1 && seen[gid_of(i)] != 0;
+    cnt += __popc(__ballot_sync(0xffffffffu, f));
+  }
+  if (lane == 0) sh.s_cnt[warp] = cnt;
+  __syncthreads();
+  if (warp == 0) {
+    const int c = sh.s_cnt[lane];
+    int x = c;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
     }
-    if (tid == 0) {
-      sh.nfront = 0;
-      sh.nb = 0;
+    sh.s_off[lane] = x - c;
+    if (lane == 31) sh.R = x;
+  }
+  __syncthreads();
+  int off = sh.s_off[warp];
+  for (int32_t b = w0; b < w1; b += 32) {
+    const int32_t i = b + lane;
+    int32_t gid = 0;
+    bool f = false;
+    if (i < w1) {
+      gid = gid_of(i);
+      f = seen[gid] != 0;
     }
-    __syncthreads();
-    bool run = true;
-    if (rs < 0 || rd < 0 || rs == rd) {
-      if (tid == 0) sh.status = OGR_NO_PATH;
-      run = false;
+    const unsigned m = __ballot_sync(0xffffffffu, f);
+    if (f) {
+      const int pos = off + __popc(m & ((1u << lane) - 1));
+      if (pos < out_cap) out[pos] = gid;
+      if (gid == src) sh.pos_src = pos;
+      if (gid == dst) sh.pos_dst = pos;
     }
-    __syncthreads();
-    if (run) {
-      if (tid == 0) {
-        w.st[rs] = ST_DONE;
-        w.lab[rs] = 0.0;
-        w.m32[rs] = 0.0f;
-        w.par[rs] = -1;
-        w.blist[0] = rs;
-        sh.nb = 1;
+    off += __popc(m);
+  }
+  __syncthreads();
+  if (tid == 0) {
+    int R = sh.R;
+    if (R > a.max_roi_nodes) {
+      // Must-keep swap (extract_roi_bfs :2359-2379): the positions of src/dst
+      // in ascending order; each one beyond the cut swaps with slot 0 / 1.
+      int kp[2];
+      int32_t kn[2];
+      int nk = 0;
+      if (src == dst) {
+        kp[0] = sh.pos_src; kn[0] = src; nk = 1;
+      } else {
+        const bool s_first = sh.pos_src < sh.pos_dst;
+        kp[0] = s_first ? sh.pos_src : sh.pos_dst; kn[0] = s_first ? src : dst;
+        kp[1] = s_first ? sh.pos_dst : sh.pos_src; kn[1] = s_first ? dst : src;
+        nk = 2;
       }
+      for (int k = 0; k < nk; ++k)
+        if (kp[k] >= a.max_roi_nodes) out[k] = kn[k];
+      R = a.max_roi_nodes;
+    }
+    sh.R = R;
+    if (sh.overflow || R > out_cap) sh.status = OGR_ERR_CAPACITY;
+    atomicAdd(&g_stage[12], (unsigned long long)R);
+  }
+  // restore seen[] to zero over the bounding box
+  for (int32_t i = tid; i < V; i += kThreads) seen[gid_of(i)] = 0;
+  __syncthreads();
+  clk.mark(1);
+}
+
+// ---- the search on a given ROI ---------------------------------------------------
+// roi[0..R) in ROI order (ignored when full).  Writes the path (global ids,
+// src first) to path_out and its length to sh.len, or a status to sh.status.
+__device__ void sssp_roi(Shared& sh, const ogr_graph& g, const ogr_state& st, const ogr_net_args& a, const Ws& w,
+                         const int32_t* roi, int32_t R, int32_t* path_out, int32_t path_cap,
+                         unsigned long long* stats_acc, StageClock& clk) {
+  const int tid = threadIdx.x;
+  const int lane = tid & 31, warp = tid >> 5;
+  const int sl = tid & (kSub - 1), grp = tid / kSub;
+  const int32_t src = a.src, dst = a.dst;
+  const bool full = a.full_graph != 0;
+  const int32_t* __restrict__ indptr = g.indptr;
+  const int32_t* __restrict__ indices = g.indices;
+  NodeSt* __restrict__ node = w.node;
+  const float kInf = __int_as_float(0x7f800000);
+
+  if (!full)
+    for (int r = tid; r < R; r += kThreads) w.g2r[roi[r]] = r;
+  if (tid == 0) {
+    sh.local = (!full && R <= kAdjCap) ? 1 : 0;
+    sh.nfront = 0;
+    sh.nb = 0;
+    sh.found = 0;
+    sh.len = 0;
+  }
+  for (int r = tid; r < R; r += kThreads) {
+    node[r].st = ST_NONE;
+    node[r].stamp = -1;
+  }
+  __syncthreads();
+  // ROI-local adjacency: neighbour ROI index and in-arc cost per slot.
+  if (sh.local) {
+    int too_wide = 0;
+    for (int r = grp; r < R; r += kGroups) {
+      const int32_t rg = roi[r];
+      const int32_t e0 = indptr[rg], e1 = indptr[rg + 1];
+      if (e1 - e0 > kDMax) too_wide = 1;
+      for (int k = sl; k < kDMax; k += kSub) {
+        const int32_t e = e0 + k;
+        int32_t u = -1;
+        float c = kInf;
+        if (e < e1) {
+          u = w.g2r[indices[e]];
+          c = st.total_cost[g.rev[e]];
+        }
+        w.adj[(int64_t)r * kDMax + k] = u;
+        w.acost[(int64_t)r * kDMax + k] = c;
+      }
+      if (sl == 0) w.deg[r] = min(e1 - e0, kDMax);
+    }
+    too_wide = __reduce_or_sync(0xffffffffu, too_wide);
+    if (lane == 0 && too_wide) sh.local = 0;
+  }
+  const int32_t rs = full ? src : w.g2r[src];
+  const int32_t rd = full ? dst : w.g2r[dst];
+  if (tid == 0 && (rs < 0 || rd < 0 || rs == rd)) sh.status = OGR_NO_PATH;
+  __syncthreads();
+  const bool local = sh.local != 0;
+  clk.mark(2);
+  int phase = 0;
+  if (sh.status == OGR_OK) {
+    if (tid == 0) {
+      node[rs].st = ST_DONE;
+      node[rs].lab = 0.0;
+      node[rs].m32 = 0.0f;
+      node[rs].par = -1;
+      w.blist[0] = rs;
+      sh.nb = 1;
+    }
+    __syncthreads();
+    int cur = 0;
+    const int max_phase = R + 2;
+    while (true) {
+      // 1. queue the unsettled ROI neighbours of the newly settled nodes
+      if (tid == 0) sh.ndirty = 0;
       __syncthreads();
-      int cur = 0;
-      int phase = 0;
-      const int max_phase = R + 2;
-      while (true) {
-        // 1. dirty = unsettled ROI neighbours of the newly settled set.
-        if (tid == 0) sh.ndirty = 0;
-        __syncthreads();
-        const int nb = sh.nb;
-        for (int i = tid; i < nb; i += kThreads) {
-          const int32_t x = w.blist[i];
-          const int32_t xg = full ? x : w.roi[x];
-          for (int32_t e = indptr[xg]; e < indptr[xg + 1]; ++e) {
+      const int nb = sh.nb;
+      for (int i = grp; i < nb; i += kGroups) {
+        const int32_t x = w.blist[i];
+        if (local) {
+          const int dx = w.deg[x];
+          for (int k = sl; k < dx; k += kSub) {
+            const int32_t y = w.adj[(int64_t)x * kDMax + k];
+            if (y < 0 || node[y].st == ST_DONE) continue;
+            if (atomicExch(&node[y].stamp, phase) != phase) w.dl[atomicAdd(&sh.ndirty, 1)] = y;
+          }
+        } else {
+          const int32_t xg = full ? x : roi[x];
+          const int32_t e1 = indptr[xg + 1];
+          for (int32_t e = indptr[xg] + sl; e < e1; e += kSub) {
             const int32_t yg = indices[e];
             const int32_t y = full ? yg : w.g2r[yg];
-            if (y < 0 || w.st[y] == ST_DONE) continue;
-            if (atomicExch(&w.dstamp[y], phase) != phase) {
-              const int p = atomicAdd(&sh.ndirty, 1);
-              w.dl[p] = y;
-            }
+            if (y < 0 || node[y].st == ST_DONE) continue;
+            if (atomicExch(&node[y].stamp, phase) != phase) w.dl[atomicAdd(&sh.ndirty, 1)] = y;
           }
-        }
-        __syncthreads();
-        // 2. recompute each dirty node from all settled in-neighbours.
-        const int nd = sh.ndirty;
-        for (int i = tid; i < nd; i += kThreads) {
-          const int32_t y = w.dl[i];
-          const int32_t yg = full ? y : w.roi[y];
-          const bool fresh = w.st[y] == ST_NONE;
-          float p;
-          if (fresh) {
-            p = node_penalty(st, a, yg);
-            w.pen[y] = p;
-          } else {
-            p = w.pen[y];
-          }
-          const double pd = (double)p;
-          Key best{__int_as_float(0x7f800000), 0.0, 0x7fffffff, 0.0};
-          bool have = false;
-          float cin = __int_as_float(0x7f800000);
-          for (int32_t e = indptr[yg]; e < indptr[yg + 1]; ++e) {
-            const int32_t ug = indices[e];
-            const int32_t u = full ? ug : w.g2r[ug];
-            if (u < 0) continue;
-            const float c = st.total_cost[g.rev[e]];
-            if (w.st[u] != ST_DONE) {
-              cin = fminf(cin, c);
-              continue;
-            }
-            const double lu = w.lab[u];
-            const double alt = (lu + (double)c) + pd;
-            const float a32 = __double2float_rn(alt);
-            if (!(a32 < __int_as_float(0x7f800000))) continue;
-            if (!have || key_less(a32, lu, u, best)) {
-              best.a32 = a32; best.lu = lu; best.u = u; best.alt = alt;
-              have = true;
-            }
-          }
-          w.cin[y] = cin;
-          if (have) {
-            w.m32[y] = best.a32;
-            w.lab[y] = best.alt;
-            w.par[y] = best.u;
-            if (fresh) {
-              w.st[y] = ST_FRONT;
-              const int q = atomicAdd(&sh.nfront, 1);
-              w.fr[cur][q] = y;
-            }
-          }
-        }
-        __syncthreads();
-        const int nf = sh.nfront;
-        if (nf == 0) {
-          if (tid == 0) sh.status = OGR_NO_PATH;
-          break;
-        }
-        // 3. T = smallest tentative label in the frontier.
-        unsigned long long mn = ~0ull;
-        for (int i = tid; i < nf; i += kThreads) {
-          const unsigned long long b = ogr_dbits(w.lab[w.fr[cur][i]]);
-          mn = b < mn ? b : mn;
-        }
-        mn = block_min_u64(mn, sh.s_min);
-        const double T = __longlong_as_double((long long)mn);
-        // 4. settle every node whose state can no longer change.
-        if (tid == 0) { sh.nb = 0; sh.nnext = 0; }
-        __syncthreads();
-        for (int i = tid; i < nf; i += kThreads) {
-          const int32_t x = w.fr[cur][i];
-          const double lx = w.lab[x];
-          bool settle = (lx == T);
-          if (!settle) {
-            const float bound = __double2float_rn((T + (double)w.cin[x]) + (double)w.pen[x]);
-            settle = w.m32[x] < bound;
-          }
-          if (settle) {
-            const int p = atomicAdd(&sh.nb, 1);
-            w.blist[p] = x;
-          } else {
-            const int p = atomicAdd(&sh.nnext, 1);
-            w.fr[cur ^ 1][p] = x;
-          }
-        }
-        __syncthreads();
-        for (int i = tid; i < sh.nb; i += kThreads) w.st[w.blist[i]] = ST_DONE;
-        if (tid == 0) sh.nfront = sh.nnext;
-        cur ^= 1;
-        __syncthreads();
-        if (w.st[rd] == ST_DONE) {
-          if (tid == 0) sh.found = 1;
-          break;
-        }
-        if (++phase > max_phase) {
-          if (tid == 0) sh.status = OGR_ERR_ITER_CAP;
-          break;
         }
       }
       __syncthreads();
-      // Arcs the sequential search scans before popping dst: the rows of all
-      // nodes popped before it, i.e. settled with (L, idx) < (L(dst), dst).
-      if (sh.found && stats_out != nullptr) {
-        if (tid == 0) { sh.total = 0; sh.nnext = 0; }
-        __syncthreads();
-        const double ld = w.lab[rd];
-        int arcs = 0, pops = 0;
-        for (int r = tid; r < R; r += kThreads) {
-          if (w.st[r] != ST_DONE) continue;
-          const double lr = w.lab[r];
-          if (lr < ld || (lr == ld && r < rd)) {
-            const int32_t rg = full ? r : w.roi[r];
-            arcs += indptr[rg + 1] - indptr[rg];
-            ++pops;
+      clk.mark(3);
+      // 2. recompute each queued node from all settled in-neighbours: a
+      //    16-lane group per node, lanes over its arcs, shuffle reduction.
+      const int nd = sh.ndirty;
+      const int half = lane >> 4;
+      for (int base = warp * 2; base < nd; base += kWarps * 2) {
+        const int idx = base + half;
+        const bool valid = idx < nd;
+        const int32_t y = valid ? w.dl[idx] : 0;
+        bool fresh = false;
+        float p = 0.0f;
+        if (valid) {
+          fresh = node[y].st == ST_NONE;
+          if (sl == 0) p = fresh ? node_penalty(st, a, full ? y : roi[y]) : node[y].pen;
+        }
+        p = __shfl_sync(0xffffffffu, p, lane & 16);
+        const double pd = (double)p;
+        float ba = kInf, bc = kInf;
+        double bl = 0.0;
+        int32_t bu = 0x7fffffff;
+        float cin = kInf;
+        if (valid) {
+          if (local) {
+            const int dy = w.deg[y];
+            for (int k = sl; k < dy; k += kSub) {
+              const int32_t u = w.adj[(int64_t)y * kDMax + k];
+              if (u < 0) continue;
+              const float c = w.acost[(int64_t)y * kDMax + k];
+              if (node[u].st != ST_DONE) {
+                cin = fminf(cin, c);
+                continue;
+              }
+              const double lu = node[u].lab;
+              const float a32 = __double2float_rn((lu + (double)c) + pd);
+              if (!(a32 < kInf)) continue;
+              if (key_lt(a32, lu, u, ba, bl, bu)) { ba = a32; bl = lu; bu = u; bc = c; }
+            }
+          } else {
+            const int32_t yg = full ? y : roi[y];
+            const int32_t e1 = indptr[yg + 1];
+            for (int32_t e = indptr[yg] + sl; e < e1; e += kSub) {
+              const int32_t ug = indices[e];
+              const int32_t u = full ? ug : w.g2r[ug];
+              if (u < 0) continue;
+              const float c = st.total_cost[g.rev[e]];
+              if (node[u].st != ST_DONE) {
+                cin = fminf(cin, c);
+                continue;
+              }
+              const double lu = node[u].lab;
+              const float a32 = __double2float_rn((lu + (double)c) + pd);
+              if (!(a32 < kInf)) continue;
+              if (key_lt(a32, lu, u, ba, bl, bu)) { ba = a32; bl = lu; bu = u; bc = c; }
+            }
           }
         }
-        atomicAdd(&sh.total, arcs);
-        atomicAdd(&sh.nnext, pops);
-        __syncthreads();
-        if (tid == 0) {
-          stats_out[0] = sh.total;
-          stats_out[1] = sh.nnext + 1;
-          stats_out[2] = R;
-          stats_out[3] = phase + 1;
+#pragma unroll
+        for (int o = 8; o > 0; o >>= 1) {
+          const float oa = __shfl_xor_sync(0xffffffffu, ba, o);
+          const double ol = __shfl_xor_sync(0xffffffffu, bl, o);
+          const int32_t ou = __shfl_xor_sync(0xffffffffu, bu, o);
+          const float oc = __shfl_xor_sync(0xffffffffu, bc, o);
+          if (key_lt(oa, ol, ou, ba, bl, bu)) { ba = oa; bl = ol; bu = ou; bc = oc; }
+          cin = fminf(cin, __shfl_xor_sync(0xffffffffu, cin, o));
+        }
+        if (valid && sl == 0) {
+          NodeSt& ns = node[y];
+          if (fresh) ns.pen = p;
+          ns.cin = cin;
+          if (ba < kInf) {
+            ns.m32 = ba;
+            ns.lab = (bl + (double)bc) + pd;
+            ns.par = bu;
+            if (fresh) {
+              ns.st = ST_FRONT;
+              w.fr[cur][atomicAdd(&sh.nfront, 1)] = y;
+            }
+          }
         }
       }
-      // Backtrace dst -> src.
-      if (tid == 0 && sh.found && sh.status == OGR_OK) {
-        int len = 0;
-        for (int32_t c = rd; c != -1 && len <= R; c = w.par[c]) ++len;
-        if (len > R) {
-          sh.status = OGR_ERR_ITER_CAP;  // parent chain longer than the ROI: a cycle
-        } else if (len > path_cap) {
-          sh.status = OGR_ERR_CAPACITY;
+      __syncthreads();
+      clk.mark(4);
+      if (tid == 0) atomicAdd(&g_stage[13], (unsigned long long)nd);
+      const int nf = sh.nfront;
+      if (nf == 0) {
+        if (tid == 0) sh.status = OGR_NO_PATH;
+        break;
+      }
+      // 3. T = smallest tentative label in the frontier.
+      unsigned long long mn = ~0ull;
+      for (int i = tid; i < nf; i += kThreads) {
+        const unsigned long long b = ogr_dbits(node[w.fr[cur][i]].lab);
+        mn = b < mn ? b : mn;
+      }
+      mn = block_min_u64(mn, sh.s_min);
+      const double T = __longlong_as_double((long long)mn);
+      clk.mark(5);
+      // 4. settle every node whose state can no longer change.
+      if (tid == 0) { sh.nb = 0; sh.nnext = 0; }
+      __syncthreads();
+      for (int i = tid; i < nf; i += kThreads) {
+        const int32_t x = w.fr[cur][i];
+        NodeSt& ns = node[x];
+        bool settle = (ns.lab == T);
+        if (!settle) settle = ns.m32 < __double2float_rn((T + (double)ns.cin) + (double)ns.pen);
+        if (settle) {
+          ns.st = ST_DONE;
+          w.blist[atomicAdd(&sh.nb, 1)] = x;
         } else {
-          int i = len - 1;
-          for (int32_t c = rd; c != -1; c = w.par[c]) path_out[i--] = full ? c : w.roi[c];
-          w.result[1] = len;
-          if (len < 2) sh.status = OGR_NO_PATH;
+          w.fr[cur ^ 1][atomicAdd(&sh.nnext, 1)] = x;
         }
       }
+      __syncthreads();
+      if (tid == 0) sh.nfront = sh.nnext;
+      cur ^= 1;
+      clk.mark(6);
+      if (tid == 0) atomicAdd(&g_stage[10], 1ull);
+      const bool done = node[rd].st == ST_DONE;
+      const bool capped = phase + 1 > max_phase;
+      __syncthreads();
+      if (done) {
+        if (tid == 0) sh.found = 1;
+        break;
+      }
+      if (capped) {
+        if (tid == 0) sh.status = OGR_ERR_ITER_CAP;
+        break;
+      }
+      ++phase;
     }
   }
   __syncthreads();
-  // ---------------------------------------------------------------- cleanup
-  if (!full) {
-    for (int r = tid; r < R; r += kThreads) w.g2r[w.roi[r]] = -1;
-    const int W = sh.bx1 - sh.bx0 + 1, H = sh.by1 - sh.by0 + 1;
-    const int64_t area = (int64_t)W * H;
-    const int64_t V = area * nz;
-    for (int64_t i = tid; i < V; i += kThreads) {
-      const int z = (int)(i / area);
-      const int64_t rem = i - (int64_t)z * area;
-      const int y = sh.by0 + (int)(rem / W);
-      const int x = sh.bx0 + (int)(rem % W);
-      w.seen[z * plane + (int64_t)y * nx + x] = 0;
+  // Arcs the sequential search scans before popping dst: the rows of all
+  // nodes popped before it, i.e. settled with (L, idx) < (L(dst), dst).
+  if (sh.found && stats_acc != nullptr) {
+    const double ld = node[rd].lab;
+    unsigned arcs = 0, pops = 0;
+    for (int r = tid; r < R; r += kThreads) {
+      if (node[r].st != ST_DONE) continue;
+      const double lr = node[r].lab;
+      if (lr < ld || (lr == ld && r < rd)) {
+        const int32_t rg = full ? r : roi[r];
+        arcs += (unsigned)(indptr[rg + 1] - indptr[rg]);
+        ++pops;
+      }
+    }
+    arcs = __reduce_add_sync(0xffffffffu, arcs);
+    pops = __reduce_add_sync(0xffffffffu, pops);
+    if (lane == 0) {
+      atomicAdd(&stats_acc[0], (unsigned long long)arcs);
+      atomicAdd(&stats_acc[1], (unsigned long long)pops);
+    }
+    if (tid == 0) {
+      atomicAdd(&stats_acc[1], 1ull);
+      atomicAdd(&stats_acc[2], (unsigned long long)R);
+      atomicAdd(&stats_acc[3], (unsigned long long)(phase + 1));
     }
   }
-  if (tid == 0) w.result[0] = sh.status;
-}
-
-__global__ void __launch_bounds__(kThreads, 1)
-find_path_kernel(ogr_graph g, ogr_state st, ogr_net_args a, Ws w, int32_t* path_out, int32_t path_cap,
-                 int64_t* stats) {
-  search_one(g, st, a, w, path_out, path_cap, false, nullptr, 0, stats);
-}
-
-__global__ void __launch_bounds__(kThreads, 1)
-roi_kernel(ogr_graph g, ogr_net_args a, Ws w, int32_t* roi_out, int32_t roi_cap) {
-  ogr_state st{};
-  search_one(g, st, a, w, nullptr, 0, true, roi_out, roi_cap, nullptr);
-}
-
-__global__ void ws_init_kernel(Ws w, int64_t N) {
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
-    w.seen[i] = 0;
-    w.g2r[i] = -1;
+  // Backtrace dst -> src.
+  if (tid == 0 && sh.found && sh.status == OGR_OK) {
+    int len = 0;
+    for (int32_t c = rd; c != -1 && len <= R; c = node[c].par) ++len;
+    if (len > R) {
+      sh.status = OGR_ERR_ITER_CAP;  // a parent chain longer than the ROI is a cycle
+    } else if (len > path_cap) {
+      sh.status = OGR_ERR_CAPACITY;
+    } else {
+      int i = len - 1;
+      for (int32_t c = rd; c != -1; c = node[c].par) path_out[i--] = full ? c : roi[c];
+      sh.len = len;
+      if (len < 2) sh.status = OGR_NO_PATH;
+    }
   }
+  __syncthreads();
+  clk.mark(7);
+  if (!full)
+    for (int r = tid; r < R; r += kThreads) w.g2r[roi[r]] = -1;
+  __syncthreads();
+  clk.mark(8);
+  if (tid == 0) atomicAdd(&g_stage[9], 1ull);
+}
+
+// Whole search for one net on one CTA (ROI extraction inline).
+__device__ void search_net(Shared& sh, const ogr_graph& g, const ogr_state& st, const ogr_net_args& a, const Ws& w,
+                           int32_t* path_out, int32_t path_cap, unsigned long long* stats_acc) {
+  StageClock clk;
+  clk.start();
+  if (threadIdx.x == 0) {
+    sh.status = OGR_OK;
+    sh.len = 0;
+    sh.found = 0;
+  }
+  __syncthreads();
+  int32_t R = g.num_nodes;
+  if (!a.full_graph) {
+    roi_build(sh, g, a, w.seen, w.q, w.qcap, w.roi, a.max_roi_nodes, clk);
+    R = sh.R;
+  }
+  if (sh.status != OGR_OK) return;
+  sssp_roi(sh, g, st, a, w, w.roi, R, path_out, path_cap, stats_acc, clk);
 }
 
 // ---- commit / rip-up ---------------------------------------------------------
-constexpr int kApplyThreads = 256;
-constexpr int kMaxViaNodes = 4096;
-
-__global__ void __launch_bounds__(kApplyThreads)
-path_apply_kernel(ogr_graph g, ogr_state st, const int32_t* path, int32_t len, int32_t net_id, int32_t sign,
-                  float pres_fac, int32_t live, int32_t* arcs_out, int32_t* status) {
-  __shared__ int32_t s_via[kMaxViaNodes];
-  __shared__ int s_nvia;
-  __shared__ int s_bad;
-  const int tid = threadIdx.x;
-  if (tid == 0) { s_nvia = 0; s_bad = 0; }
+// commit_path / clear_path (:1096-1135) + refresh_live_present_costs (:1403),
+// _mark/_clear_path_node_use (:4635-4659), barrel ownership of every node a
+// via hop spans (:4934-5034), arcs in _path_to_edges order (:9981-10046).
+// Returns OGR_OK, OGR_ERR_ARG (a hop is not an arc) or OGR_ERR_CAPACITY.
+__device__ int apply_path_dev(const ogr_graph& g, const ogr_state& st, const int32_t* path, int32_t len,
+                              int32_t net_id, int32_t sign, float pres_fac, int32_t live, int32_t* arcs_out,
+                              int32_t* s_via, int* s_flags) {
+  const int tid = threadIdx.x, nt = blockDim.x;
+  if (tid == 0) { s_flags[0] = 0; s_flags[1] = 0; }
   __syncthreads();
   const int hops = len - 1;
-  const int64_t plane = (int64_t)g.nx * g.ny;
-  // Arcs: forward hop i is path[i]->path[i+1]; the reversed path's hop j is
-  // the opposite arc of forward hop hops-1-j (_path_to_edges order).
-  for (int i = tid; i < hops; i += kApplyThreads) {
+  const int32_t plane = g.nx * g.ny;
+  for (int i = tid; i < hops; i += nt) {
     const int32_t u = path[i], v = path[i + 1];
     int32_t f = -1;
     for (int32_t e = g.indptr[u]; e < g.indptr[u + 1]; ++e)
       if (g.indices[e] == v) { f = e; break; }
-    if (f < 0) { s_bad = 1; continue; }
+    if (f < 0) { s_flags[1] = 1; continue; }
     const int32_t r = g.rev[f];
     const int j = hops - 1 - i;
     if (arcs_out) { arcs_out[i] = f; arcs_out[hops + j] = r; }
@@ -586,45 +733,257 @@ path_apply_kernel(ogr_graph g, ogr_state st, const int32_t* path, int32_t len, i
       }
     }
   }
-  // Path-node use (a simple path visits each node once).
-  for (int i = tid; i < len; i += kApplyThreads) {
+  for (int i = tid; i < len; i += nt) {
     const int32_t n = path[i];
     const int32_t u = st.path_node_use[n];
     st.path_node_use[n] = sign > 0 ? u + 1 : max(u - 1, 0);
   }
   __syncthreads();
-  // Barrel ownership: union of the z-ranges of all via hops (deduplicated).
   if (tid == 0) {
     int nv = 0;
-    for (int i = 0; i < hops && !s_bad; ++i) {
+    for (int i = 0; i < hops && !s_flags[1]; ++i) {
       const int32_t u = path[i], v = path[i + 1];
-      const int64_t ru = u % plane, rv = v % plane;
-      const int zu = (int)(u / plane), zv = (int)(v / plane);
+      const int32_t ru = u % plane, rv = v % plane;
+      const int zu = u / plane, zv = v / plane;
       if (ru != rv || zu == zv) continue;
       for (int z = min(zu, zv); z <= max(zu, zv); ++z) {
-        const int32_t node = (int32_t)(z * plane + ru);
+        const int32_t nd = z * plane + ru;
         bool dup = false;
         for (int k = 0; k < nv; ++k)
-          if (s_via[k] == node) { dup = true; break; }
+          if (s_via[k] == nd) { dup = true; break; }
         if (dup) continue;
-        if (nv >= kMaxViaNodes) { s_bad = 2; break; }
-        s_via[nv++] = node;
+        if (nv >= kMaxViaNodes) { s_flags[1] = 2; break; }
+        s_via[nv++] = nd;
       }
     }
-    s_nvia = nv;
+    s_flags[0] = nv;
   }
   __syncthreads();
-  for (int k = tid; k < s_nvia; k += kApplyThreads) {
-    const int32_t node = s_via[k];
-    st.owner_count[node] += sign > 0 ? 1 : -1;
-    st.owner_xor[node] ^= net_id;
+  const int nv = s_flags[0];
+  for (int k = tid; k < nv; k += nt) {
+    const int32_t nd = s_via[k];
+    st.owner_count[nd] += sign > 0 ? 1 : -1;
+    st.owner_xor[nd] ^= net_id;
   }
-  if (tid == 0) *status = s_bad ? (s_bad == 1 ? OGR_ERR_ARG : OGR_ERR_CAPACITY) : OGR_OK;
+  const int bad = s_flags[1];
+  __syncthreads();
+  return bad ? (bad == 1 ? OGR_ERR_ARG : OGR_ERR_CAPACITY) : OGR_OK;
+}
+
+// ---- kernels -------------------------------------------------------------------
+__global__ void __launch_bounds__(kThreads, 1)
+find_path_kernel(ogr_graph g, ogr_state st, ogr_net_args a, Ws w, int32_t* path_out, int32_t path_cap,
+                 int64_t* stats) {
+  __shared__ Shared sh;
+  search_net(sh, g, st, a, w, path_out, path_cap, reinterpret_cast<unsigned long long*>(stats));
+  if (threadIdx.x == 0) {
+    w.result[0] = sh.status;
+    w.result[1] = sh.len;
+  }
+}
+
+__global__ void __launch_bounds__(kThreads, 1)
+roi_kernel(ogr_graph g, ogr_net_args a, Ws w, int32_t* roi_out, int32_t roi_cap) {
+  __shared__ Shared sh;
+  StageClock clk;
+  clk.start();
+  if (threadIdx.x == 0) sh.status = OGR_OK;
+  __syncthreads();
+  int R = 0;
+  if (a.full_graph) {
+    R = g.num_nodes;
+    if (threadIdx.x == 0 && R > roi_cap) sh.status = OGR_ERR_CAPACITY;
+    __syncthreads();
+    if (sh.status == OGR_OK)
+      for (int r = threadIdx.x; r < R; r += kThreads) roi_out[r] = r;
+  } else {
+    roi_build(sh, g, a, w.seen, w.q, w.qcap, roi_out, roi_cap, clk);
+    R = sh.R;
+  }
+  if (threadIdx.x == 0) {
+    w.result[0] = sh.status;
+    w.result[1] = R;
+  }
+}
+
+__global__ void ws_init_kernel(Ws w, int64_t N) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
+    w.seen[i] = 0;
+    w.g2r[i] = -1;
+  }
+}
+
+__global__ void bfs_init_kernel(char* base, int32_t slots, size_t slot_bytes, int32_t N, int64_t qcap) {
+  for (int s = 0; s < slots; ++s) {
+    BfsSlot b = bfs_slot_at(base + (size_t)s * slot_bytes, N, qcap);
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x)
+      b.seen[i] = 0;
+  }
+}
+
+constexpr int kApplyThreads = 256;
+
+__global__ void __launch_bounds__(kApplyThreads)
+path_apply_kernel(ogr_graph g, ogr_state st, const int32_t* path, int32_t len, int32_t net_id, int32_t sign,
+                  float pres_fac, int32_t live, int32_t* arcs_out, int32_t* status) {
+  __shared__ int32_t s_via[kMaxViaNodes];
+  __shared__ int s_flags[2];
+  const int rc = apply_path_dev(g, st, path, len, net_id, sign, pres_fac, live, arcs_out, s_via, s_flags);
+  if (threadIdx.x == 0) *status = rc;
+}
+
+__device__ inline ogr_net_args pass_net_args(const ogr_net_table& t, const ogr_pass_args& pa, int32_t n,
+                                             int fallback) {
+  ogr_net_args a;
+  a.net_id = t.net_id[n];
+  a.src = t.net_src[n];
+  a.dst = t.net_dst[n];
+  a.full_graph = fallback ? 0 : t.net_full[n];
+  a.bfs_max_depth = t.net_depth[2 * n + fallback];
+  a.bfs_halo = t.net_halo[2 * n + fallback];
+  a.bfs_stop_count = pa.bfs_stop_count;
+  a.max_roi_nodes = pa.max_roi_nodes;
+  a.owner_weight = pa.owner_weight;
+  a.path_weight = pa.path_weight;
+  a.history_weight = pa.history_weight;
+  a.penalty_enabled = pa.penalty_enabled;
+  return a;
+}
+
+// Extract the (cost-independent) ROIs of every ROI net of the pass, one net
+// per CTA at a time, each CTA with its own BFS slot.  roi_len[n] = -1 when a
+// queue overflowed (the pass then extracts that ROI inline).
+__global__ void __launch_bounds__(kThreads, 1)
+roi_batch_kernel(ogr_graph g, ogr_net_table t, ogr_pass_args pa, ogr_roi_batch rb) {
+  __shared__ Shared sh;
+  __shared__ int s_k;
+  BfsSlot slot = bfs_slot_at((char*)rb.bfs_ws + (size_t)blockIdx.x * rb.slot_bytes, g.num_nodes, rb.qcap);
+  while (true) {
+    if (threadIdx.x == 0) s_k = atomicAdd(rb.next, 1);
+    __syncthreads();
+    const int k = s_k;
+    __syncthreads();
+    if (k >= pa.count) break;
+    const int32_t n = pa.order[k];
+    if (t.net_full[n]) {
+      if (threadIdx.x == 0) rb.roi_len[n] = 0;
+      continue;
+    }
+    ogr_net_args a = pass_net_args(t, pa, n, 0);
+    StageClock clk;
+    clk.start();
+    if (threadIdx.x == 0) sh.status = OGR_OK;
+    __syncthreads();
+    roi_build(sh, g, a, slot.seen, slot.q, slot.qcap, rb.roi_pool + (int64_t)n * rb.roi_cap, rb.roi_cap, clk);
+    if (threadIdx.x == 0) rb.roi_len[n] = (sh.status == OGR_OK) ? sh.R : -1;
+    __syncthreads();
+  }
+}
+
+// One launch routes an ordered list of nets the way _route_all does.
+__global__ void __launch_bounds__(kThreads, 1)
+route_pass_kernel(ogr_graph g, ogr_state st, ogr_net_table t, ogr_pass_args pa, ogr_roi_batch rb, int use_batch,
+                  Ws w) {
+  __shared__ Shared sh;
+  __shared__ int32_t s_via[kMaxViaNodes];
+  __shared__ int s_flags[2];
+  __shared__ int s_fallbacks;
+  __shared__ int s_error;
+  unsigned long long* stats = reinterpret_cast<unsigned long long*>(pa.stats);
+  if (threadIdx.x == 0) { s_fallbacks = 0; s_error = OGR_OK; }
+  __syncthreads();
+  for (int k = 0; k < pa.count; ++k) {
+    const int32_t n = pa.order[k];
+    int32_t* slot = t.store_path + (int64_t)n * t.slot_cap;
+    int32_t* arcs = t.store_arcs + (int64_t)n * 2 * t.slot_cap;
+    const int32_t old_len = t.store_len[n];
+    if (old_len >= 2) {
+      const int rc = apply_path_dev(g, st, slot, old_len, t.net_id[n], -1, pa.pres_fac, pa.live, nullptr, s_via,
+                                    s_flags);
+      if (rc != OGR_OK) {
+        if (threadIdx.x == 0) s_error = rc;
+        break;
+      }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) t.store_len[n] = 0;
+    ogr_net_args a = pass_net_args(t, pa, n, 0);
+    const int pre = (use_batch && !a.full_graph) ? rb.roi_len[n] : -1;
+    if (pre > 0) {
+      StageClock clk;
+      clk.start();
+      if (threadIdx.x == 0) {
+        sh.status = OGR_OK;
+        atomicAdd(&g_stage[14], 1ull);
+      }
+      __syncthreads();
+      sssp_roi(sh, g, st, a, w, rb.roi_pool + (int64_t)n * rb.roi_cap, pre, slot, t.slot_cap, stats, clk);
+    } else {
+      search_net(sh, g, st, a, w, slot, t.slot_cap, stats);
+    }
+    int flags = 0;
+    const int st1 = sh.status;
+    if (st1 < 0) {
+      if (threadIdx.x == 0) s_error = st1;
+      break;
+    }
+    if (st1 != OGR_OK && s_fallbacks < pa.fallback_quota) {
+      a = pass_net_args(t, pa, n, 1);
+      __syncthreads();
+      if (threadIdx.x == 0) ++s_fallbacks;
+      search_net(sh, g, st, a, w, slot, t.slot_cap, stats);
+      const int st2 = sh.status;
+      if (st2 < 0) {
+        if (threadIdx.x == 0) s_error = st2;
+        break;
+      }
+      flags |= 2;
+    }
+    const int fin = sh.status;
+    const int len = sh.len;
+    __syncthreads();
+    if (fin == OGR_OK) {
+      const int rc = apply_path_dev(g, st, slot, len, t.net_id[n], +1, pa.pres_fac, pa.live, arcs, s_via, s_flags);
+      if (rc != OGR_OK) {
+        if (threadIdx.x == 0) s_error = rc;
+        break;
+      }
+      if (threadIdx.x == 0) t.store_len[n] = len;
+    } else {
+      flags |= 1;
+    }
+    if (threadIdx.x == 0) pa.net_status[k] = flags;
+    __syncthreads();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) w.result[0] = s_error;
 }
 
 }  // namespace
 
 extern "C" size_t ogr_route_workspace_bytes(int32_t num_nodes) { return ws_layout(num_nodes, nullptr, nullptr); }
+
+extern "C" size_t ogr_bfs_workspace_bytes(int32_t num_nodes, int64_t qcap, int32_t slots) {
+  return bfs_slot_bytes(num_nodes, qcap) * (size_t)slots;
+}
+
+extern "C" int ogr_bfs_workspace_init(void* ws, int32_t num_nodes, int64_t qcap, int32_t slots, void* stream) {
+  if (!ws || slots < 1 || qcap < 1) return OGR_ERR_ARG;
+  bfs_init_kernel<<<ogr_blocks(num_nodes, 256), 256, 0, ogr_stream(stream)>>>(
+      (char*)ws, slots, bfs_slot_bytes(num_nodes, qcap), num_nodes, qcap);
+  OGR_LAUNCH_CHECK();
+  return OGR_OK;
+}
+
+extern "C" int ogr_search_profile(int64_t* out16, int32_t reset) {
+  if (!out16) return OGR_ERR_ARG;
+  OGR_CUDA_TRY(cudaMemcpyFromSymbol(out16, g_stage, sizeof(unsigned long long) * 16));
+  if (reset) {
+    unsigned long long z[16] = {};
+    OGR_CUDA_TRY(cudaMemcpyToSymbol(g_stage, z, sizeof(z)));
+  }
+  return OGR_OK;
+}
 
 extern "C" int ogr_route_workspace_init(void* ws, size_t bytes, int32_t N, void* stream) {
   if (!ws || bytes < ogr_route_workspace_bytes(N)) return OGR_ERR_CAPACITY;
@@ -657,6 +1016,8 @@ extern "C" int ogr_extract_roi(const ogr_graph* g, const ogr_net_args* net, void
                                int32_t* roi_out, int32_t roi_cap, int32_t* roi_len_out, void* stream) {
   if (!g || !net || !ws || !roi_out || !roi_len_out) return OGR_ERR_ARG;
   if (bytes < ogr_route_workspace_bytes(g->num_nodes)) return OGR_ERR_CAPACITY;
+  if (!net->full_graph && roi_cap < (net->max_roi_nodes < g->num_nodes ? net->max_roi_nodes : g->num_nodes))
+    return OGR_ERR_ARG;
   Ws w;
   ws_layout(g->num_nodes, (char*)ws, &w);
   cudaStream_t s = ogr_stream(stream);
@@ -679,6 +1040,40 @@ extern "C" int ogr_path_apply(const ogr_graph* g, const ogr_state* st, const int
   return OGR_OK;
 }
 
+extern "C" int ogr_route_pass(const ogr_graph* g, const ogr_state* st, const ogr_net_table* t,
+                              const ogr_pass_args* pa, const ogr_roi_batch* rb, void* ws, size_t bytes,
+                              int32_t* status_out, void* stream) {
+  if (!g || !st || !t || !pa || !ws || !status_out) return OGR_ERR_ARG;
+  if (bytes < ogr_route_workspace_bytes(g->num_nodes)) return OGR_ERR_CAPACITY;
+  if (pa->count < 0 || t->slot_cap < 2) return OGR_ERR_ARG;
+  if (pa->count == 0) {
+    *status_out = OGR_OK;
+    return OGR_OK;
+  }
+  if (!pa->order || !pa->net_status || !pa->stats) return OGR_ERR_ARG;
+  const bool batch = rb != nullptr && rb->slots > 0;
+  const int32_t need_cap = pa->max_roi_nodes < g->num_nodes ? pa->max_roi_nodes : g->num_nodes;
+  if (batch && (!rb->bfs_ws || !rb->roi_pool || !rb->roi_len || !rb->next || rb->roi_cap < need_cap))
+    return OGR_ERR_ARG;
+  Ws w;
+  ws_layout(g->num_nodes, (char*)ws, &w);
+  cudaStream_t s = ogr_stream(stream);
+  ogr_roi_batch rbv{};
+  if (batch) {
+    rbv = *rb;
+    OGR_CUDA_TRY(cudaMemsetAsync(rbv.next, 0, sizeof(int32_t), s));
+    roi_batch_kernel<<<rbv.slots, kThreads, 0, s>>>(*g, *t, *pa, rbv);
+    OGR_LAUNCH_CHECK();
+  }
+  route_pass_kernel<<<1, kThreads, 0, s>>>(*g, *st, *t, *pa, rbv, batch ? 1 : 0, w);
+  OGR_LAUNCH_CHECK();
+  int64_t res;
+  OGR_CUDA_TRY(cudaMemcpyAsync(&res, w.result, sizeof(res), cudaMemcpyDeviceToHost, s));
+  OGR_CUDA_TRY(cudaStreamSynchronize(s));
+  *status_out = (int32_t)res;
+  return res < 0 ? (int)res : OGR_OK;
+}
+
 // ---- allocation-free search ----------------------------------------------------
 // Some hosts cannot hand this library a workspace: a plugin loaded into an
 // application that owns the device allocator, or a serving process that
@@ -698,15 +1093,7 @@ extern "C" int ogr_path_apply(const ogr_graph* g, const ogr_state* st, const int
 //    another host thread) race on it — serialise them.
 namespace {
 
-constexpr size_t noalloc_round(size_t v) { return (v + 255) & ~(size_t)255; }
-
-constexpr size_t noalloc_ws_bytes() {
-  // The layout of ws_layout() for OGR_NOALLOC_MAX_NODES nodes: 16 int32 /
-  // float arrays, one double array, one byte array, the 64-byte result block,
-  // each rounded up to 256 bytes (about 19 MB).
-  return 16 * noalloc_round((size_t)OGR_NOALLOC_MAX_NODES * 4) + noalloc_round((size_t)OGR_NOALLOC_MAX_NODES * 8) +
-         noalloc_round((size_t)OGR_NOALLOC_MAX_NODES) + noalloc_round(64);
-}
+constexpr size_t noalloc_ws_bytes() { return ws_bytes_for((size_t)OGR_NOALLOC_MAX_NODES); }
 
 static __device__ __align__(256) unsigned char g_noalloc_ws[noalloc_ws_bytes()];
 

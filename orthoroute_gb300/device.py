@@ -240,3 +240,79 @@ class Ops:
         if int(self.status.item()) != 0:
             raise ValueError("path hop is not a graph edge")
         return out
+
+
+class PathStore:
+    """Device-resident current path of every net of a job (one fixed slot each),
+    plus the per-net ROI pool and BFS slots of the batched ROI extraction."""
+
+    def __init__(self, graph: DeviceGraph, num_nets: int, slot_cap: int = 8192, max_roi_nodes: int = 50_000,
+                 bfs_slots: int = 64):
+        dev = graph.device
+        lib = graph.lib
+        self.num_nets = num_nets
+        self.slot_cap = slot_cap
+        self.length = torch.zeros(num_nets, dtype=torch.int32, device=dev)
+        self.path = torch.zeros((num_nets, slot_cap), dtype=torch.int32, device=dev)
+        self.arcs = torch.zeros((num_nets, 2 * slot_cap), dtype=torch.int32, device=dev)
+        N = graph.N
+        self.roi_cap = int(min(max_roi_nodes, N))
+        self.roi_pool = torch.zeros((num_nets, self.roi_cap), dtype=torch.int32, device=dev)
+        self.roi_len = torch.zeros(num_nets, dtype=torch.int32, device=dev)
+        self.next = torch.zeros(1, dtype=torch.int32, device=dev)
+        self.bfs_slots = int(max(1, min(bfs_slots, num_nets)))
+        self.qcap = int(min(N, max(4 * max_roi_nodes, 1 << 18)))
+        per = int(lib.ogr_bfs_workspace_bytes(N, self.qcap, 1))
+        self.slot_bytes = per
+        self.bfs_ws = torch.empty(per * self.bfs_slots, dtype=torch.uint8, device=dev)
+        _lib.check(lib.ogr_bfs_workspace_init(_p(self.bfs_ws), N, self.qcap, self.bfs_slots, None),
+                   "ogr_bfs_workspace_init")
+
+    def roi_batch(self) -> _lib.RoiBatch:
+        return _lib.RoiBatch(self.bfs_slots, self.slot_bytes, self.qcap, _p(self.bfs_ws), _p(self.roi_pool),
+                             _p(self.roi_len), self.roi_cap, _p(self.next))
+
+    def set_path(self, idx: int, path):
+        n = len(path)
+        if n > self.slot_cap:
+            raise RuntimeError("path longer than the path-store slot")
+        if n:
+            self.path[idx, :n] = torch.as_tensor(np.asarray(path, dtype=np.int32)).to(self.path.device)
+        self.length[idx] = n if n >= 2 else 0
+
+
+def route_pass(ops: "Ops", store: PathStore, table: dict, order: np.ndarray, *, fallback_quota, max_roi_nodes,
+               owner_weight, path_weight, history_weight, pres_fac, live, penalty=True, batch_roi=True):
+    """One ``ogr_route_pass`` launch; returns (per-net status flags, stats[4])."""
+    dev = ops.g.device
+    k = len(order)
+    if k == 0:
+        return np.zeros(0, dtype=np.int32), np.zeros(4, dtype=np.int64)
+    d_order = torch.as_tensor(np.asarray(order, dtype=np.int32)).to(dev)
+    status = torch.zeros(max(k, 1), dtype=torch.int32, device=dev)
+    stats = torch.zeros(4, dtype=torch.int64, device=dev)
+    t = _lib.NetTable(store.num_nets, store.slot_cap, _p(store.length), _p(store.path), _p(store.arcs),
+                      _p(table["src"]), _p(table["dst"]), _p(table["id"]), _p(table["full"]), _p(table["depth"]),
+                      _p(table["halo"]))
+    a = _lib.PassArgs(_p(d_order), k, int(fallback_quota), int(max_roi_nodes), float(max_roi_nodes) * 1.5,
+                      float(np.float32(owner_weight)), float(np.float32(path_weight)),
+                      float(np.float32(history_weight)), int(bool(penalty)), float(np.float32(pres_fac)),
+                      int(bool(live)), _p(status), _p(stats))
+    g = ops.g.cgraph()
+    st = ops.s.cstate()
+    rc_dev = C.c_int32(0)
+    stream = ops.stream if ops.stream is not None else torch.cuda.current_stream()
+    ops._ev0.record(stream)
+    rb = store.roi_batch() if batch_roi else None
+    rc = ops.lib.ogr_route_pass(C.byref(g), C.byref(st), C.byref(t), C.byref(a),
+                                C.byref(rb) if rb is not None else None, _p(ops.ws[0]), ops.ws_bytes,
+                                C.byref(rc_dev), ops._sp())
+    ops._ev1.record(stream)
+    _lib.check(rc, "ogr_route_pass")
+    ops._ev1.synchronize()
+    ops.counters["search_ms"] += ops._ev0.elapsed_time(ops._ev1)
+    ops.counters["search_launches"] += 1
+    ops.counters["launches"] += 1
+    ops.counters["h2d_bytes"] += 4 * k
+    ops.counters["d2h_bytes"] += 4 * k + 32
+    return status[:k].cpu().numpy(), stats.cpu().numpy()

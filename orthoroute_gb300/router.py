@@ -33,7 +33,7 @@ import numpy as np
 import torch
 
 from . import _lib
-from .device import DeviceGraph, DeviceState, Ops, require_cuda
+from .device import DeviceGraph, DeviceState, Ops, PathStore, require_cuda, route_pass
 from .lattice import Lattice, default_layer_dirs
 
 ROI_THRESHOLD_STEPS = 125
@@ -267,10 +267,14 @@ class PathFinderRouter:
     """GB300 PathFinder router with the reference's Python API."""
 
     def __init__(self, config: Optional[PathFinderConfig] = None, use_gpu: Optional[bool] = None,
-                 device: str = "cuda"):
+                 device: str = "cuda", mode: str = "persistent"):
         require_cuda()
+        if mode not in ("persistent", "plain"):
+            raise ValueError("mode must be 'persistent' (one launch per routing pass) or 'plain' (one per net)")
         self.config = config or PathFinderConfig()
         self.device = device
+        self.mode = mode
+        self.store: Optional[PathStore] = None
         self.lattice: Optional[Lattice] = None
         self.net_paths: Dict[str, List[int]] = {}
         self.iteration = 0
@@ -726,6 +730,8 @@ class PathFinderRouter:
     def _apply(self, name, path, sign, live):
         edges = self.ops.apply_path(path, self._net_id(name), sign, self._present_pres_fac, live=live)
         self._mark_nodes(name, path, sign)
+        if self.store is not None:
+            self.store.set_path(self._task_index[name], path if sign > 0 else [])
         return edges
 
     def _order_nets(self, tasks):
@@ -759,6 +765,8 @@ class PathFinderRouter:
         live = bool(cfg.live_present_costs)
         if live:
             self.ops.live_begin(self._present_pres_fac)
+        if self.mode == "persistent":
+            return self._route_all_pass(tasks, all_tasks, ordered, bonus, live)
         for name in ordered:
             src, dst = tasks[name]
             if name in self.net_paths and self.net_paths[name]:
@@ -780,6 +788,75 @@ class PathFinderRouter:
             else:
                 self.net_paths[name] = []
                 self._clear_tracking(name)
+        routed = sum(1 for p in self.net_paths.values() if p)
+        return routed, len(all_tasks) - routed
+
+    def _net_table(self, bonus):
+        """Per-net search parameters of this pass (``extract_roi`` :2240-2255)."""
+        names = self._task_names
+        n = len(names)
+        src = np.empty(n, dtype=np.int32)
+        dst = np.empty(n, dtype=np.int32)
+        nid = np.empty(n, dtype=np.int32)
+        full = np.empty(n, dtype=np.int32)
+        depth = np.empty(2 * n, dtype=np.int32)
+        halo = np.empty(2 * n, dtype=np.int32)
+        for i, name in enumerate(names):
+            s_, d_ = self._tasks_all[name]
+            src[i], dst[i] = s_, d_
+            nid[i] = self._net_id(name)
+            dist = self._manhattan(s_, d_)
+            full[i] = 1 if dist >= ROI_THRESHOLD_STEPS else 0
+            for j, b in enumerate((bonus, bonus * 2)):
+                radius = max(60, int(dist * 0.75 + b * 2.0))
+                depth[2 * i + j] = min(int(radius + b * 2.0), 80)
+                halo[2 * i + j] = min(16, 2 + int(max(0.0, b) / 0.6))
+        dev = self.g.device
+        return {k: torch.from_numpy(v).to(dev) for k, v in
+                dict(src=src, dst=dst, id=nid, full=full, depth=depth, halo=halo).items()}
+
+    def _route_all_pass(self, tasks, all_tasks, ordered, bonus, live):
+        """The per-net loop of ``_route_all`` as one device launch."""
+        cfg = self.config
+        for name in ordered:
+            self._net_id(name)
+        table = self._net_table(bonus)
+        order = np.asarray([self._task_index[n] for n in ordered], dtype=np.int32)
+        w = float(cfg.owner_penalty_base) * float(self._pres_fac_now)
+        if self.freeze:
+            w = max(w, float(cfg.portal_cleanup_node_penalty))
+        t0 = time.perf_counter()
+        status, st = route_pass(self.ops, self.store, table, order, fallback_quota=5, max_roi_nodes=MAX_ROI_NODES,
+                                owner_weight=w, path_weight=float(cfg.path_node_penalty_base) * float(self._pres_fac_now),
+                                history_weight=cfg.node_history_penalty, pres_fac=self._present_pres_fac, live=live)
+        self.stats["search_s"] += time.perf_counter() - t0
+        self.stats["searches"] += len(ordered) + int(np.count_nonzero(status & 2))
+        self.stats["arcs"] += int(st[0])
+        self.stats["pops"] += int(st[1])
+        self.full_graph_fallback_count = int(np.count_nonzero(status & 2))
+        lengths = self.store.length.cpu().numpy()
+        idx = torch.as_tensor(order.astype(np.int64), device=self.g.device)
+        L = int(lengths[order].max()) if len(order) else 0
+        rows = self.store.path[idx, :max(L, 1)].cpu().numpy() if len(order) else None
+        arow = self.store.arcs[idx, :max(2 * (L - 1), 1)].cpu().numpy() if len(order) else None
+        self.ops.counters["d2h_bytes"] += 4 * lengths.size + (rows.nbytes + arow.nbytes if rows is not None else 0)
+        for k, name in enumerate(ordered):
+            old = self.net_paths.get(name)
+            if old:
+                self._mark_nodes(name, old, -1)
+                self._clear_tracking(name)
+            n = int(lengths[order[k]])
+            if not (status[k] & 1) and n >= 2:
+                path = rows[k, :n].tolist()
+                edges = arow[k, :2 * (n - 1)].tolist()
+                self._mark_nodes(name, path, +1)
+                self.net_paths[name] = path
+                self._update_tracking(name, edges)
+            else:
+                self.net_paths[name] = []
+                self._clear_tracking(name)
+            if self.search_log is not None:
+                self.search_log.append((self.iteration, name, "pass", self.net_paths[name] or None))
         routed = sum(1 for p in self.net_paths.values() if p)
         return routed, len(all_tasks) - routed
 
@@ -952,6 +1029,8 @@ class PathFinderRouter:
         self.members = {}
         self.net_to_edges.clear()
         self.edge_to_nets.clear()
+        if self.store is not None:
+            self.store.length.zero_()
         for n, p in self.net_paths.items():
             if not p or len(p) < 2:
                 continue
@@ -1042,6 +1121,13 @@ class PathFinderRouter:
         if self.lattice is None:
             raise RuntimeError("initialize_graph() first")
         tasks = self._parse_requests(requests)
+        self._tasks_all = tasks
+        self._task_names = list(tasks)
+        self._task_index = {n: i for i, n in enumerate(self._task_names)}
+        if self.mode == "persistent":
+            if self.store is None or self.store.num_nets != len(tasks):
+                self.store = PathStore(self.g, len(tasks))
+            self.store.length.zero_()
         self._edge_src_host = self.g.edge_src.cpu().numpy()
         self._indices_host = self.g.indices.cpu().numpy()
         self._edge_layer_host = self.g.edge_layer.cpu().numpy()

@@ -30,20 +30,21 @@ def flat(paths):
     return np.asarray(out, dtype=np.int64)
 
 
-def gpu_router(nx, ny, nz, iters):
+def gpu_router(nx, ny, nz, iters, mode="persistent"):
     from orthoroute_gb300 import Lattice
     from orthoroute_gb300.router import PathFinderConfig, PathFinderRouter
-    R = PathFinderRouter(PathFinderConfig(max_iterations=iters))
+    R = PathFinderRouter(PathFinderConfig(max_iterations=iters), mode=mode)
     R.initialize_lattice(Lattice(nx, ny, nz), board_bounds(nx, ny))
     return R
 
 
+@pytest.mark.parametrize("mode", ["persistent", "plain"])
 @pytest.mark.parametrize("tag", ["r0", "r1"])
-def test_gpu_router_matches_reference_runs(tag):
+def test_gpu_router_matches_reference_runs(tag, mode):
     m = META[tag]
     z = np.load(os.path.join(G, "runs.npz"))
     reqs = [(f"N{int(r[0])}", int(r[1]), int(r[2])) for r in z[f"{tag}_reqs"]]
-    R = gpu_router(m["nx"], m["ny"], m["nz"], m["iters"])
+    R = gpu_router(m["nx"], m["ny"], m["nz"], m["iters"], mode)
     R.trace = []
     res = R.route_multiple_nets(reqs)
     n_ref = sum(1 for k in z.files if k.startswith(f"{tag}_it"))
@@ -67,14 +68,16 @@ def seeded_nets(nx, ny, n, seed, dmin=5, dmax=80):
     return out
 
 
-@pytest.mark.parametrize("dims,n_nets,iters,seed", [((40, 36, 6), 60, 8, 7), ((48, 40, 8), 90, 10, 11)])
-def test_gpu_router_matches_oracle_loop(dims, n_nets, iters, seed):
+@pytest.mark.parametrize("mode", ["persistent", "plain"])
+@pytest.mark.parametrize("dims,n_nets,iters,seed", [((40, 36, 6), 60, 8, 7), ((48, 40, 8), 90, 10, 11),
+                                                    ((140, 40, 6), 40, 6, 5)])
+def test_gpu_router_matches_oracle_loop(dims, n_nets, iters, seed, mode):
     nx, ny, nz = dims
-    reqs = seeded_nets(nx, ny, n_nets, seed)
-    R = gpu_router(nx, ny, nz, iters)
+    reqs = seeded_nets(nx, ny, n_nets, seed, dmin=5, dmax=160)
+    R = gpu_router(nx, ny, nz, iters, mode)
     R.trace = []
     res = R.route_multiple_nets(reqs)
-    O = OracleRouter(LatticeSpec(nx, ny, nz), board_bounds(nx, ny), Config(max_iterations=iters))
+    O = OracleRouter(LatticeSpec(nx, ny, nz), board_bounds(nx, ny), Config(max_iterations=iters), fast=True)
     O.trace = []
     ores = O.route({n: (s, d) for n, s, d in reqs})
     assert len(R.trace) == len(O.trace)
