@@ -31,7 +31,8 @@ enum {
   OGR_ERR_CUDA = -2,
   OGR_ERR_CAPACITY = -3,  /* a queue, ROI or path buffer is too small     */
   OGR_ERR_ITER_CAP = -4,  /* a device loop reached its iteration limit     */
-  OGR_ERR_NUMERIC = -5    /* an input violated an exactness precondition  */
+  OGR_ERR_NUMERIC = -5,   /* an input violated an exactness precondition  */
+  OGR_ERR_TIMEOUT = -6    /* a grid-wide barrier gave up waiting           */
 };
 
 /* ------------------------------------------------------------------ A1 ---
@@ -277,10 +278,38 @@ size_t ogr_bfs_workspace_bytes(int32_t num_nodes, int64_t qcap, int32_t slots);
 int ogr_bfs_workspace_init(void* workspace, int32_t num_nodes, int64_t qcap, int32_t slots,
                            void* stream);
 
-/* rb may be NULL (every ROI is extracted inline, in order). */
+/* rb may be NULL (every ROI is extracted inline, in order).
+ * order_full (HOST uint8[count], may be NULL) marks the entries of `order`
+ * that are full-graph nets; each of those is searched by the whole-lattice
+ * search (ogr_find_path_full) in full_workspace, the ROI nets between them by
+ * single-CTA launches, in the same order.  With order_full NULL every net,
+ * long or not, is searched by the single-CTA pass. */
 int ogr_route_pass(const ogr_graph* g, const ogr_state* st, const ogr_net_table* t,
                    const ogr_pass_args* pa, const ogr_roi_batch* rb, void* workspace,
-                   size_t workspace_bytes, int32_t* status_out, void* stream);
+                   size_t workspace_bytes, const uint8_t* order_full, void* full_workspace,
+                   size_t full_workspace_bytes, int32_t* status_out, void* stream);
+
+/* Whole-lattice search for nets with Manhattan length >= 125 (the
+ * reference's full-graph branch of _route_all, unified_pathfinder.py:
+ * 8219-8262, into find_path_roi :2451-2548 with roi_nodes = all nodes).  Same
+ * result, statistics and status codes as ogr_find_path with
+ * net->full_graph = 1, computed by one cooperative launch on all SMs.  The
+ * workspace (about 44 bytes per node + 4 per arc) is initialised once with
+ * ogr_full_workspace_init; searches then touch only the nodes they reach.
+ * OGR_ERR_TIMEOUT: a grid barrier gave up (not expected; the launch is
+ * sized so every CTA is resident).  Synchronises. */
+size_t ogr_full_workspace_bytes(int32_t num_nodes, int64_t num_edges);
+int ogr_full_workspace_init(void* workspace, size_t workspace_bytes, int32_t num_nodes,
+                            int64_t num_edges, void* stream);
+int ogr_find_path_full(const ogr_graph* g, const ogr_state* st, const ogr_net_args* net,
+                       void* workspace, size_t workspace_bytes, int32_t* path_out,
+                       int32_t path_cap, int32_t* path_len_out, int64_t* stats, void* stream);
+
+/* Tracing of the whole-lattice search (host int64[8], cumulative since the
+ * last reset): searches, phases, kernel ns, init ns, E-step work ns and
+ * S-step work ns of the busiest CTA, barrier wait ns and statistics +
+ * backtrace ns of CTA 0.  Synchronous. */
+int ogr_full_profile(int64_t* out8, int32_t reset);
 
 /* Tracing: cumulative per-stage cycle counters of all searches on the
  * current device since the last reset (host int64[16]: BFS, compaction,

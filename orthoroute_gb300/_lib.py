@@ -16,7 +16,8 @@ OGR_NO_PATH = 1
 OGR_ERR_CAPACITY = -3
 OGR_NOALLOC_MAX_NODES = 262144
 ERRORS = {-1: "bad argument", -2: "CUDA error", -3: "buffer capacity exceeded",
-          -4: "device loop iteration limit reached", -5: "exactness precondition violated"}
+          -4: "device loop iteration limit reached", -5: "exactness precondition violated",
+          -6: "grid barrier timed out"}
 
 EXPORTED = [
     "ogr_csr_num_edges", "ogr_csr_workspace_bytes", "ogr_csr_build",
@@ -24,7 +25,8 @@ EXPORTED = [
     "ogr_tally", "ogr_route_workspace_bytes", "ogr_route_workspace_init",
     "ogr_find_path", "ogr_path_apply", "ogr_extract_roi", "ogr_via_pools_apply", "ogr_overused_arcs",
     "ogr_find_path_noalloc", "ogr_route_pass", "ogr_search_profile", "ogr_bfs_workspace_bytes",
-    "ogr_bfs_workspace_init",
+    "ogr_bfs_workspace_init", "ogr_full_workspace_bytes", "ogr_find_path_full",
+    "ogr_full_profile", "ogr_full_workspace_init",
 ]
 
 P = C.c_void_p
@@ -120,7 +122,12 @@ def load(build_if_missing: bool = True):
                                   C.POINTER(I32), P, P],
         "ogr_search_profile": [P, I32],
         "ogr_route_pass": [C.POINTER(Graph), C.POINTER(State), C.POINTER(NetTable), C.POINTER(PassArgs),
-                           C.POINTER(RoiBatch), P, C.c_size_t, C.POINTER(I32), P],
+                           C.POINTER(RoiBatch), P, C.c_size_t, P, P, C.c_size_t, C.POINTER(I32), P],
+        "ogr_full_workspace_bytes": [I32, I64],
+        "ogr_full_profile": [P, I32],
+        "ogr_full_workspace_init": [P, C.c_size_t, I32, I64, P],
+        "ogr_find_path_full": [C.POINTER(Graph), C.POINTER(State), C.POINTER(NetArgs), P, C.c_size_t, P, I32,
+                               C.POINTER(I32), P, P],
         "ogr_bfs_workspace_bytes": [I32, I64, I32],
         "ogr_bfs_workspace_init": [P, I32, I64, I32, P],
     }

@@ -25,3 +25,43 @@ static inline int ogr_blocks(int64_t n, int threads, int cap = 152 * 16) {
 __device__ __forceinline__ unsigned long long ogr_dbits(double d) {
   return (unsigned long long)__double_as_longlong(d);
 }
+
+// Node penalty of the search (_build_owner_penalty, unified_pathfinder.py:
+// 5308-5384): foreign barrel owner + occupied path node + history, float32.
+__device__ __forceinline__ float ogr_node_penalty(const ogr_state& st, const ogr_net_args& a, int32_t gid) {
+  if (!a.penalty_enabled) return 0.0f;
+  const int32_t cnt = st.owner_count[gid];
+  const int32_t owner = (cnt == 0) ? -1 : (cnt == 1 ? st.owner_xor[gid] : -2);
+  const bool foreign = (owner != -1) && (owner != a.net_id);
+  const bool occupied = st.path_node_use[gid] > 0;
+  const float f = foreign ? a.owner_weight : 0.0f;
+  const float o = occupied ? a.path_weight : 0.0f;
+  return __fadd_rn(__fadd_rn(f, o), __fmul_rn(st.node_history[gid], a.history_weight));
+}
+
+// (a32, lu, u) lexicographic less-than.
+__device__ __forceinline__ bool ogr_key_lt(float a1, double l1, int32_t u1, float a2, double l2, int32_t u2) {
+  if (a1 != a2) return a1 < a2;
+  if (l1 != l2) return l1 < l2;
+  return u1 < u2;
+}
+
+// Search parameters of net n of a pass (fallback = 1: the larger retry ROI).
+__device__ inline ogr_net_args ogr_pass_net_args(const ogr_net_table& t, const ogr_pass_args& pa, int32_t n,
+                                             int fallback) {
+  ogr_net_args a;
+  a.net_id = t.net_id[n];
+  a.src = t.net_src[n];
+  a.dst = t.net_dst[n];
+  a.full_graph = fallback ? 0 : t.net_full[n];
+  a.bfs_max_depth = t.net_depth[2 * n + fallback];
+  a.bfs_halo = t.net_halo[2 * n + fallback];
+  a.bfs_stop_count = pa.bfs_stop_count;
+  a.max_roi_nodes = pa.max_roi_nodes;
+  a.owner_weight = pa.owner_weight;
+  a.path_weight = pa.path_weight;
+  a.history_weight = pa.history_weight;
+  a.penalty_enabled = pa.penalty_enabled;
+  return a;
+}
+

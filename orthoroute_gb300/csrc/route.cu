@@ -36,6 +36,7 @@
 // fallbacks left, commit) for a whole ordered list of nets in one launch,
 // with every net's current path kept in a device-resident store.
 #include "common.cuh"
+#include "fullgraph.cuh"
 
 namespace {
 
@@ -159,24 +160,6 @@ __device__ __forceinline__ unsigned long long block_min_u64(unsigned long long v
   unsigned long long r = s[0];
   __syncthreads();
   return r;
-}
-
-__device__ __forceinline__ float node_penalty(const ogr_state& st, const ogr_net_args& a, int32_t gid) {
-  if (!a.penalty_enabled) return 0.0f;
-  const int32_t cnt = st.owner_count[gid];
-  const int32_t owner = (cnt == 0) ? -1 : (cnt == 1 ? st.owner_xor[gid] : -2);
-  const bool foreign = (owner != -1) && (owner != a.net_id);
-  const bool occupied = st.path_node_use[gid] > 0;
-  const float f = foreign ? a.owner_weight : 0.0f;
-  const float o = occupied ? a.path_weight : 0.0f;
-  return __fadd_rn(__fadd_rn(f, o), __fmul_rn(st.node_history[gid], a.history_weight));
-}
-
-// (a32, lu, u) lexicographic less-than.
-__device__ __forceinline__ bool key_lt(float a1, double l1, int32_t u1, float a2, double l2, int32_t u2) {
-  if (a1 != a2) return a1 < a2;
-  if (l1 != l2) return l1 < l2;
-  return u1 < u2;
 }
 
 // Per-stage cycle counters of the search (a tracing aid, read with
@@ -469,7 +452,12 @@ __device__ void sssp_roi(Shared& sh, const ogr_graph& g, const ogr_state& st, co
     }
     __syncthreads();
     int cur = 0;
-    const int max_phase = R + 2;
+    const int max_phase = 2 * R + 4;
+    // With statistics requested the search goes on after dst is settled until
+    // every node with a label <= L(dst) is settled (T > L(dst)): the IN bound
+    // can settle dst before cheaper nodes, which the heap pops earlier.
+    bool dst_done = false;
+    double ld_stop = 0.0;
     while (true) {
       // 1. queue the unsettled ROI neighbours of the newly settled nodes
       if (tid == 0) sh.ndirty = 0;
@@ -509,7 +497,7 @@ __device__ void sssp_roi(Shared& sh, const ogr_graph& g, const ogr_state& st, co
         float p = 0.0f;
         if (valid) {
           fresh = node[y].st == ST_NONE;
-          if (sl == 0) p = fresh ? node_penalty(st, a, full ? y : roi[y]) : node[y].pen;
+          if (sl == 0) p = fresh ? ogr_node_penalty(st, a, full ? y : roi[y]) : node[y].pen;
         }
         p = __shfl_sync(0xffffffffu, p, lane & 16);
         const double pd = (double)p;
@@ -531,7 +519,7 @@ __device__ void sssp_roi(Shared& sh, const ogr_graph& g, const ogr_state& st, co
               const double lu = node[u].lab;
               const float a32 = __double2float_rn((lu + (double)c) + pd);
               if (!(a32 < kInf)) continue;
-              if (key_lt(a32, lu, u, ba, bl, bu)) { ba = a32; bl = lu; bu = u; bc = c; }
+              if (ogr_key_lt(a32, lu, u, ba, bl, bu)) { ba = a32; bl = lu; bu = u; bc = c; }
             }
           } else {
             const int32_t yg = full ? y : roi[y];
@@ -548,7 +536,7 @@ __device__ void sssp_roi(Shared& sh, const ogr_graph& g, const ogr_state& st, co
               const double lu = node[u].lab;
               const float a32 = __double2float_rn((lu + (double)c) + pd);
               if (!(a32 < kInf)) continue;
-              if (key_lt(a32, lu, u, ba, bl, bu)) { ba = a32; bl = lu; bu = u; bc = c; }
+              if (ogr_key_lt(a32, lu, u, ba, bl, bu)) { ba = a32; bl = lu; bu = u; bc = c; }
             }
           }
         }
@@ -558,7 +546,7 @@ __device__ void sssp_roi(Shared& sh, const ogr_graph& g, const ogr_state& st, co
           const double ol = __shfl_xor_sync(0xffffffffu, bl, o);
           const int32_t ou = __shfl_xor_sync(0xffffffffu, bu, o);
           const float oc = __shfl_xor_sync(0xffffffffu, bc, o);
-          if (key_lt(oa, ol, ou, ba, bl, bu)) { ba = oa; bl = ol; bu = ou; bc = oc; }
+          if (ogr_key_lt(oa, ol, ou, ba, bl, bu)) { ba = oa; bl = ol; bu = ou; bc = oc; }
           cin = fminf(cin, __shfl_xor_sync(0xffffffffu, cin, o));
         }
         if (valid && sl == 0) {
@@ -581,7 +569,12 @@ __device__ void sssp_roi(Shared& sh, const ogr_graph& g, const ogr_state& st, co
       if (tid == 0) atomicAdd(&g_stage[13], (unsigned long long)nd);
       const int nf = sh.nfront;
       if (nf == 0) {
-        if (tid == 0) sh.status = OGR_NO_PATH;
+        if (tid == 0) {
+          if (dst_done)
+            sh.found = 1;
+          else
+            sh.status = OGR_NO_PATH;
+        }
         break;
       }
       // 3. T = smallest tentative label in the frontier.
@@ -593,6 +586,10 @@ __device__ void sssp_roi(Shared& sh, const ogr_graph& g, const ogr_state& st, co
       mn = block_min_u64(mn, sh.s_min);
       const double T = __longlong_as_double((long long)mn);
       clk.mark(5);
+      if (dst_done && T > ld_stop) {
+        if (tid == 0) sh.found = 1;
+        break;
+      }
       // 4. settle every node whose state can no longer change.
       if (tid == 0) { sh.nb = 0; sh.nnext = 0; }
       __syncthreads();
@@ -613,12 +610,16 @@ __device__ void sssp_roi(Shared& sh, const ogr_graph& g, const ogr_state& st, co
       cur ^= 1;
       clk.mark(6);
       if (tid == 0) atomicAdd(&g_stage[10], 1ull);
-      const bool done = node[rd].st == ST_DONE;
+      const bool done = !dst_done && node[rd].st == ST_DONE;
       const bool capped = phase + 1 > max_phase;
+      if (done) ld_stop = node[rd].lab;
       __syncthreads();
       if (done) {
-        if (tid == 0) sh.found = 1;
-        break;
+        dst_done = true;
+        if (stats_acc == nullptr) {
+          if (tid == 0) sh.found = 1;
+          break;
+        }
       }
       if (capped) {
         if (tid == 0) sh.status = OGR_ERR_ITER_CAP;
@@ -832,24 +833,6 @@ path_apply_kernel(ogr_graph g, ogr_state st, const int32_t* path, int32_t len, i
   if (threadIdx.x == 0) *status = rc;
 }
 
-__device__ inline ogr_net_args pass_net_args(const ogr_net_table& t, const ogr_pass_args& pa, int32_t n,
-                                             int fallback) {
-  ogr_net_args a;
-  a.net_id = t.net_id[n];
-  a.src = t.net_src[n];
-  a.dst = t.net_dst[n];
-  a.full_graph = fallback ? 0 : t.net_full[n];
-  a.bfs_max_depth = t.net_depth[2 * n + fallback];
-  a.bfs_halo = t.net_halo[2 * n + fallback];
-  a.bfs_stop_count = pa.bfs_stop_count;
-  a.max_roi_nodes = pa.max_roi_nodes;
-  a.owner_weight = pa.owner_weight;
-  a.path_weight = pa.path_weight;
-  a.history_weight = pa.history_weight;
-  a.penalty_enabled = pa.penalty_enabled;
-  return a;
-}
-
 // Extract the (cost-independent) ROIs of every ROI net of the pass, one net
 // per CTA at a time, each CTA with its own BFS slot.  roi_len[n] = -1 when a
 // queue overflowed (the pass then extracts that ROI inline).
@@ -869,7 +852,7 @@ roi_batch_kernel(ogr_graph g, ogr_net_table t, ogr_pass_args pa, ogr_roi_batch r
       if (threadIdx.x == 0) rb.roi_len[n] = 0;
       continue;
     }
-    ogr_net_args a = pass_net_args(t, pa, n, 0);
+    ogr_net_args a = ogr_pass_net_args(t, pa, n, 0);
     StageClock clk;
     clk.start();
     if (threadIdx.x == 0) sh.status = OGR_OK;
@@ -890,7 +873,8 @@ route_pass_kernel(ogr_graph g, ogr_state st, ogr_net_table t, ogr_pass_args pa, 
   __shared__ int s_fallbacks;
   __shared__ int s_error;
   unsigned long long* stats = reinterpret_cast<unsigned long long*>(pa.stats);
-  if (threadIdx.x == 0) { s_fallbacks = 0; s_error = OGR_OK; }
+  if (w.result[0] < 0) return;  // an earlier step of this pass failed
+  if (threadIdx.x == 0) { s_fallbacks = (int)w.result[2]; s_error = OGR_OK; }
   __syncthreads();
   for (int k = 0; k < pa.count; ++k) {
     const int32_t n = pa.order[k];
@@ -907,7 +891,7 @@ route_pass_kernel(ogr_graph g, ogr_state st, ogr_net_table t, ogr_pass_args pa, 
     }
     __syncthreads();
     if (threadIdx.x == 0) t.store_len[n] = 0;
-    ogr_net_args a = pass_net_args(t, pa, n, 0);
+    ogr_net_args a = ogr_pass_net_args(t, pa, n, 0);
     const int pre = (use_batch && !a.full_graph) ? rb.roi_len[n] : -1;
     if (pre > 0) {
       StageClock clk;
@@ -928,7 +912,7 @@ route_pass_kernel(ogr_graph g, ogr_state st, ogr_net_table t, ogr_pass_args pa, 
       break;
     }
     if (st1 != OGR_OK && s_fallbacks < pa.fallback_quota) {
-      a = pass_net_args(t, pa, n, 1);
+      a = ogr_pass_net_args(t, pa, n, 1);
       __syncthreads();
       if (threadIdx.x == 0) ++s_fallbacks;
       search_net(sh, g, st, a, w, slot, t.slot_cap, stats);
@@ -956,7 +940,76 @@ route_pass_kernel(ogr_graph g, ogr_state st, ogr_net_table t, ogr_pass_args pa, 
     __syncthreads();
   }
   __syncthreads();
-  if (threadIdx.x == 0) w.result[0] = s_error;
+  if (threadIdx.x == 0) {
+    w.result[2] = s_fallbacks;
+    if (s_error != OGR_OK) w.result[0] = s_error;
+  }
+}
+
+// Long nets of a pass run as three launches each: this rip-up, the
+// whole-lattice search on every SM (fullgraph.cu), then pass_full_tail_kernel.
+__global__ void __launch_bounds__(kThreads, 1)
+pass_ripup_kernel(ogr_graph g, ogr_state st, ogr_net_table t, ogr_pass_args pa, int32_t k, Ws w) {
+  __shared__ int32_t s_via[kMaxViaNodes];
+  __shared__ int s_flags[2];
+  if (w.result[0] < 0) return;
+  const int32_t n = pa.order[k];
+  const int32_t old_len = t.store_len[n];
+  if (old_len >= 2) {
+    const int rc = apply_path_dev(g, st, t.store_path + (int64_t)n * t.slot_cap, old_len, t.net_id[n], -1,
+                                  pa.pres_fac, pa.live, nullptr, s_via, s_flags);
+    if (rc != OGR_OK) {
+      if (threadIdx.x == 0) w.result[0] = rc;
+      return;
+    }
+  }
+  if (threadIdx.x == 0) t.store_len[n] = 0;
+}
+
+// After the whole-lattice search of net order[k]: the fallback ROI search if
+// it failed and the pass has fallbacks left, then the commit.
+__global__ void __launch_bounds__(kThreads, 1)
+pass_full_tail_kernel(ogr_graph g, ogr_state st, ogr_net_table t, ogr_pass_args pa, int32_t k, Ws w,
+                      const int32_t* full_res) {
+  __shared__ Shared sh;
+  __shared__ int32_t s_via[kMaxViaNodes];
+  __shared__ int s_flags[2];
+  if (w.result[0] < 0) return;
+  const int32_t n = pa.order[k];
+  int32_t* slot = t.store_path + (int64_t)n * t.slot_cap;
+  int32_t* arcs = t.store_arcs + (int64_t)n * 2 * t.slot_cap;
+  int fin = full_res[0];
+  int len = full_res[1];
+  if (fin < 0) {
+    if (threadIdx.x == 0) w.result[0] = fin;
+    return;
+  }
+  int flags = 0;
+  const int used = (int)w.result[2];
+  if (fin != OGR_OK && used < pa.fallback_quota) {
+    const ogr_net_args a = ogr_pass_net_args(t, pa, n, 1);
+    search_net(sh, g, st, a, w, slot, t.slot_cap, reinterpret_cast<unsigned long long*>(pa.stats));
+    fin = sh.status;
+    len = sh.len;
+    if (fin < 0) {
+      if (threadIdx.x == 0) w.result[0] = fin;
+      return;
+    }
+    flags |= 2;
+    if (threadIdx.x == 0) w.result[2] = used + 1;
+  }
+  __syncthreads();
+  if (fin == OGR_OK) {
+    const int rc = apply_path_dev(g, st, slot, len, t.net_id[n], +1, pa.pres_fac, pa.live, arcs, s_via, s_flags);
+    if (rc != OGR_OK) {
+      if (threadIdx.x == 0) w.result[0] = rc;
+      return;
+    }
+    if (threadIdx.x == 0) t.store_len[n] = len;
+  } else {
+    flags |= 1;
+  }
+  if (threadIdx.x == 0) pa.net_status[k] = flags;
 }
 
 }  // namespace
@@ -1042,7 +1095,8 @@ extern "C" int ogr_path_apply(const ogr_graph* g, const ogr_state* st, const int
 
 extern "C" int ogr_route_pass(const ogr_graph* g, const ogr_state* st, const ogr_net_table* t,
                               const ogr_pass_args* pa, const ogr_roi_batch* rb, void* ws, size_t bytes,
-                              int32_t* status_out, void* stream) {
+                              const uint8_t* order_full, void* full_ws, size_t full_bytes, int32_t* status_out,
+                              void* stream) {
   if (!g || !st || !t || !pa || !ws || !status_out) return OGR_ERR_ARG;
   if (bytes < ogr_route_workspace_bytes(g->num_nodes)) return OGR_ERR_CAPACITY;
   if (pa->count < 0 || t->slot_cap < 2) return OGR_ERR_ARG;
@@ -1055,9 +1109,16 @@ extern "C" int ogr_route_pass(const ogr_graph* g, const ogr_state* st, const ogr
   const int32_t need_cap = pa->max_roi_nodes < g->num_nodes ? pa->max_roi_nodes : g->num_nodes;
   if (batch && (!rb->bfs_ws || !rb->roi_pool || !rb->roi_len || !rb->next || rb->roi_cap < need_cap))
     return OGR_ERR_ARG;
+  bool any_full = false;
+  if (order_full)
+    for (int32_t k = 0; k < pa->count; ++k) any_full = any_full || order_full[k] != 0;
+  if (any_full && (!full_ws || full_bytes < ogr_full::workspace_bytes(g->num_nodes, g->num_edges)))
+    return OGR_ERR_CAPACITY;
   Ws w;
   ws_layout(g->num_nodes, (char*)ws, &w);
   cudaStream_t s = ogr_stream(stream);
+  // result[0] = first error of the pass, result[2] = fallbacks used so far
+  OGR_CUDA_TRY(cudaMemsetAsync(w.result, 0, 64, s));
   ogr_roi_batch rbv{};
   if (batch) {
     rbv = *rb;
@@ -1065,8 +1126,43 @@ extern "C" int ogr_route_pass(const ogr_graph* g, const ogr_state* st, const ogr
     roi_batch_kernel<<<rbv.slots, kThreads, 0, s>>>(*g, *t, *pa, rbv);
     OGR_LAUNCH_CHECK();
   }
-  route_pass_kernel<<<1, kThreads, 0, s>>>(*g, *st, *t, *pa, rbv, batch ? 1 : 0, w);
-  OGR_LAUNCH_CHECK();
+  if (!any_full) {
+    route_pass_kernel<<<1, kThreads, 0, s>>>(*g, *st, *t, *pa, rbv, batch ? 1 : 0, w);
+    OGR_LAUNCH_CHECK();
+  } else {
+    // Runs of ROI nets go through one single-CTA launch each; every long net
+    // gets the whole GPU for its search.  Same order, same state updates.
+    int32_t* full_res = ogr_full::result_words(full_ws, g->num_nodes, g->num_edges);
+    int32_t k = 0;
+    while (k < pa->count) {
+      if (order_full[k]) {
+        pass_ripup_kernel<<<1, kThreads, 0, s>>>(*g, *st, *t, *pa, k, w);
+        OGR_LAUNCH_CHECK();
+        ogr_full::Job job{};
+        job.from_pass = 1;
+        job.t = *t;
+        job.pa = *pa;
+        job.k = k;
+        job.pass_result = w.result;
+        job.stats = reinterpret_cast<unsigned long long*>(pa->stats);
+        const int rc = ogr_full::launch(*g, *st, job, full_ws, s);
+        if (rc != OGR_OK) return rc;
+        pass_full_tail_kernel<<<1, kThreads, 0, s>>>(*g, *st, *t, *pa, k, w, full_res);
+        OGR_LAUNCH_CHECK();
+        ++k;
+      } else {
+        int32_t k1 = k;
+        while (k1 < pa->count && !order_full[k1]) ++k1;
+        ogr_pass_args seg = *pa;
+        seg.order = pa->order + k;
+        seg.count = k1 - k;
+        seg.net_status = pa->net_status + k;
+        route_pass_kernel<<<1, kThreads, 0, s>>>(*g, *st, *t, seg, rbv, batch ? 1 : 0, w);
+        OGR_LAUNCH_CHECK();
+        k = k1;
+      }
+    }
+  }
   int64_t res;
   OGR_CUDA_TRY(cudaMemcpyAsync(&res, w.result, sizeof(res), cudaMemcpyDeviceToHost, s));
   OGR_CUDA_TRY(cudaStreamSynchronize(s));

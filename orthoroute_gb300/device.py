@@ -123,6 +123,8 @@ class Ops:
         self.tally_out = torch.zeros(5, dtype=torch.int64, device=graph.device)
         self.layer_units = torch.zeros(graph.lattice.nz, dtype=torch.int64, device=graph.device)
         self.counters = dict(launches=0, h2d_bytes=0, d2h_bytes=0, search_launches=0, search_ms=0.0)
+        self._full_ws = None
+        self.full_ws_bytes = 0
         self._ev0 = torch.cuda.Event(enable_timing=True)
         self._ev1 = torch.cuda.Event(enable_timing=True)
 
@@ -193,17 +195,36 @@ class Ops:
                             float(np.float32(float(path_base) * float(pres_fac))), float(np.float32(hist_pen)),
                             int(bool(penalty)))
 
-    def find_path(self, net: _lib.NetArgs, slot: int = 0) -> Optional[List[int]]:
+    def full_workspace(self) -> torch.Tensor:
+        """Workspace of the whole-lattice search (allocated on first use)."""
+        if self._full_ws is None:
+            self.full_ws_bytes = int(self.lib.ogr_full_workspace_bytes(self.g.N, self.g.E))
+            self._full_ws = torch.empty(self.full_ws_bytes, dtype=torch.uint8, device=self.g.device)
+            _lib.check(self.lib.ogr_full_workspace_init(_p(self._full_ws), self.full_ws_bytes, self.g.N, self.g.E,
+                                                        self._sp()), "ogr_full_workspace_init")
+        return self._full_ws
+
+    def find_path(self, net: _lib.NetArgs, slot: int = 0, engine: str = "auto") -> Optional[List[int]]:
+        """Search one net.  engine: "grid" = whole-lattice search on all SMs
+        (full-graph nets), "cta" = one CTA, "auto" = grid for full-graph nets."""
         g = self.g.cgraph()
         st = self.s.cstate()
         n = C.c_int32(0)
         stream = self.stream if self.stream is not None else torch.cuda.current_stream()
+        grid = engine == "grid" or (engine == "auto" and bool(net.full_graph))
+        if grid:
+            ws = self.full_workspace()
         self._ev0.record(stream)
-        rc = self.lib.ogr_find_path(C.byref(g), C.byref(st), C.byref(net), _p(self.ws[slot]), self.ws_bytes,
-                                    _p(self.path_buf), int(self.path_buf.numel()), C.byref(n), _p(self.stats),
-                                    self._sp())
+        if grid:
+            rc = self.lib.ogr_find_path_full(C.byref(g), C.byref(st), C.byref(net), _p(ws), self.full_ws_bytes,
+                                             _p(self.path_buf), int(self.path_buf.numel()), C.byref(n),
+                                             _p(self.stats), self._sp())
+        else:
+            rc = self.lib.ogr_find_path(C.byref(g), C.byref(st), C.byref(net), _p(self.ws[slot]), self.ws_bytes,
+                                        _p(self.path_buf), int(self.path_buf.numel()), C.byref(n),
+                                        _p(self.stats), self._sp())
         self._ev1.record(stream)
-        _lib.check(rc, "ogr_find_path")
+        _lib.check(rc, "ogr_find_path_full" if grid else "ogr_find_path")
         self._ev1.synchronize()
         self.counters["search_ms"] += self._ev0.elapsed_time(self._ev1)
         self.counters["search_launches"] += 1
@@ -282,8 +303,12 @@ class PathStore:
 
 
 def route_pass(ops: "Ops", store: PathStore, table: dict, order: np.ndarray, *, fallback_quota, max_roi_nodes,
-               owner_weight, path_weight, history_weight, pres_fac, live, penalty=True, batch_roi=True):
-    """One ``ogr_route_pass`` launch; returns (per-net status flags, stats[4])."""
+               owner_weight, path_weight, history_weight, pres_fac, live, penalty=True, batch_roi=True,
+               order_full: Optional[np.ndarray] = None):
+    """One ``ogr_route_pass`` call; returns (per-net status flags, stats[4]).
+
+    order_full (host, one flag per entry of order) sends the full-graph nets
+    to the whole-lattice search; None keeps every net on the single-CTA pass."""
     dev = ops.g.device
     k = len(order)
     if k == 0:
@@ -304,8 +329,14 @@ def route_pass(ops: "Ops", store: PathStore, table: dict, order: np.ndarray, *, 
     stream = ops.stream if ops.stream is not None else torch.cuda.current_stream()
     ops._ev0.record(stream)
     rb = store.roi_batch() if batch_roi else None
+    full_flags = None
+    full_ws, full_bytes = None, 0
+    if order_full is not None and np.any(order_full):
+        full_flags = np.ascontiguousarray(order_full, dtype=np.uint8)
+        full_ws, full_bytes = _p(ops.full_workspace()), ops.full_ws_bytes
     rc = ops.lib.ogr_route_pass(C.byref(g), C.byref(st), C.byref(t), C.byref(a),
                                 C.byref(rb) if rb is not None else None, _p(ops.ws[0]), ops.ws_bytes,
+                                full_flags.ctypes.data if full_flags is not None else None, full_ws, full_bytes,
                                 C.byref(rc_dev), ops._sp())
     ops._ev1.record(stream)
     _lib.check(rc, "ogr_route_pass")

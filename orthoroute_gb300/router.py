@@ -267,13 +267,16 @@ class PathFinderRouter:
     """GB300 PathFinder router with the reference's Python API."""
 
     def __init__(self, config: Optional[PathFinderConfig] = None, use_gpu: Optional[bool] = None,
-                 device: str = "cuda", mode: str = "persistent"):
+                 device: str = "cuda", mode: str = "persistent", full_engine: str = "grid"):
         require_cuda()
         if mode not in ("persistent", "plain"):
             raise ValueError("mode must be 'persistent' (one launch per routing pass) or 'plain' (one per net)")
+        if full_engine not in ("grid", "cta"):
+            raise ValueError("full_engine must be 'grid' (all SMs per full-graph net) or 'cta' (one CTA)")
         self.config = config or PathFinderConfig()
         self.device = device
         self.mode = mode
+        self.full_engine = full_engine
         self.store: Optional[PathStore] = None
         self.lattice: Optional[Lattice] = None
         self.net_paths: Dict[str, List[int]] = {}
@@ -713,7 +716,7 @@ class PathFinderRouter:
             path_base=cfg.path_node_penalty_base, hist_pen=cfg.node_history_penalty,
             freeze_weight=cfg.portal_cleanup_node_penalty if self.freeze else None, penalty=True)
         t = time.perf_counter()
-        path = self.ops.find_path(net)
+        path = self.ops.find_path(net, engine=self.full_engine if full_graph else "cta")
         self.stats["search_s"] += time.perf_counter() - t
         self.stats["searches"] += 1
         st = self.ops.stats.cpu().numpy()
@@ -812,8 +815,10 @@ class PathFinderRouter:
                 depth[2 * i + j] = min(int(radius + b * 2.0), 80)
                 halo[2 * i + j] = min(16, 2 + int(max(0.0, b) / 0.6))
         dev = self.g.device
-        return {k: torch.from_numpy(v).to(dev) for k, v in
-                dict(src=src, dst=dst, id=nid, full=full, depth=depth, halo=halo).items()}
+        table = {k: torch.from_numpy(v).to(dev) for k, v in
+                 dict(src=src, dst=dst, id=nid, full=full, depth=depth, halo=halo).items()}
+        table["full_host"] = full.astype(np.uint8)
+        return table
 
     def _route_all_pass(self, tasks, all_tasks, ordered, bonus, live):
         """The per-net loop of ``_route_all`` as one device launch."""
@@ -826,9 +831,11 @@ class PathFinderRouter:
         if self.freeze:
             w = max(w, float(cfg.portal_cleanup_node_penalty))
         t0 = time.perf_counter()
+        order_full = table["full_host"][order] if self.full_engine == "grid" else None
         status, st = route_pass(self.ops, self.store, table, order, fallback_quota=5, max_roi_nodes=MAX_ROI_NODES,
                                 owner_weight=w, path_weight=float(cfg.path_node_penalty_base) * float(self._pres_fac_now),
-                                history_weight=cfg.node_history_penalty, pres_fac=self._present_pres_fac, live=live)
+                                history_weight=cfg.node_history_penalty, pres_fac=self._present_pres_fac, live=live,
+                                order_full=order_full)
         self.stats["search_s"] += time.perf_counter() - t0
         self.stats["searches"] += len(ordered) + int(np.count_nonzero(status & 2))
         self.stats["arcs"] += int(st[0])

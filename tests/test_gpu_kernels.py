@@ -12,7 +12,7 @@ import torch
 pytestmark = pytest.mark.gpu
 
 from oracle import accounting as oacc
-from oracle.dijkstra import find_path_roi
+from oracle.dijkstra import find_path_roi, find_path_roi_c
 from oracle.lattice import LatticeSpec, build_csr
 from oracle.roi import extract_roi_bfs, roi_radius
 from oracle.tallies import NodeState, path_to_edges
@@ -218,14 +218,20 @@ def test_find_path_matches_oracle(seed):
         r = roi_radius(src, dst, ref.nx, ref.plane)
         roi, g2r = extract_roi_bfs(ref.indptr, ref.indices, N, src, dst, initial_radius=r)
         pen = ns.owner_penalty(roi, net_id, pres_fac) if ns is not None else None
-        want = find_path_roi(ref.indptr, ref.indices, src, dst, costs, roi, g2r, node_penalty=pen)
+        st = {}
+        want = find_path_roi(ref.indptr, ref.indices, src, dst, costs, roi, g2r, node_penalty=pen, stats=st)
         net = ops.net_args(net_id, src, dst, max_depth=min(r, 80), halo=2, pres_fac=pres_fac,
                            penalty=ns is not None)
+        ops.stats.zero_()
         got = ops.find_path(net)
         assert got == want, (seed, src, dst)
+        if want is not None:
+            arcs, pops, roi_n, _ = ops.stats.cpu().tolist()
+            assert (arcs, pops, roi_n) == (st["scanned"], st["settled"], len(roi)), (seed, src, dst)
 
 
-def test_find_path_full_graph_matches_oracle():
+@pytest.mark.parametrize("engine", ["grid", "cta"])
+def test_find_path_full_graph_matches_oracle(engine):
     g, s, ops, ref = make(60, 30, 6)
     rng = np.random.default_rng(9)
     costs = (np.float32(0.12) + oacc.jitter(g.E)).astype(np.float32)
@@ -235,8 +241,73 @@ def test_find_path_full_graph_matches_oracle():
     for _ in range(3):
         src, dst = (int(v) for v in rng.integers(0, ref.plane, size=2))
         want = find_path_roi(ref.indptr, ref.indices, src, dst, costs, ident, ident)
-        got = ops.find_path(ops.net_args(0, src, dst, full_graph=True, penalty=False))
+        got = ops.find_path(ops.net_args(0, src, dst, full_graph=True, penalty=False), engine=engine)
         assert got == want
+
+
+def _costs(kind, E, rng):
+    if kind == 0:
+        return (0.12 + rng.random(E) * 0.05).astype(np.float32)
+    if kind == 1:   # heavy ties
+        return (0.12 + rng.integers(0, 3, size=E) * 0.01).astype(np.float32)
+    if kind == 2:   # blocked arcs
+        c = (0.12 + rng.random(E) * 0.02).astype(np.float32)
+        c[rng.choice(E, size=E // 10, replace=False)] = np.float32("inf")
+        return c
+    return (np.float32(0.12) + oacc.jitter(E)).astype(np.float32)   # base + jitter
+
+
+@pytest.mark.parametrize("seed", range(8))
+def test_full_grid_search_matches_oracle(seed):
+    """Whole-lattice search on all SMs: paths and heap statistics vs the oracle."""
+    dims = [(80, 60, 8), (120, 40, 6), (64, 64, 12), (200, 150, 4)][seed % 4]
+    g, s, ops, ref = make(*dims)
+    rng = np.random.default_rng(100 + seed)
+    costs = _costs(seed % 4, g.E, rng)
+    s.total_cost.copy_(torch.from_numpy(costs))
+    N = g.N
+    ident = np.arange(N, dtype=np.int32)
+    net_id = 3
+    ns = _penalty_state(s, N, rng, net_id) if seed % 2 == 0 else None
+    pres_fac = float(rng.choice([1.0, 2.3, 40.0]))
+    pen = ns.owner_penalty(ident, net_id, pres_fac) if ns is not None else None
+    for _ in range(3):
+        src, dst = (int(v) for v in rng.integers(0, ref.plane, size=2))
+        st = {}
+        want = find_path_roi_c(ref.indptr, ref.indices, src, dst, costs, ident, ident, node_penalty=pen, stats=st)
+        ops.stats.zero_()
+        got = ops.find_path(ops.net_args(net_id, src, dst, full_graph=True, pres_fac=pres_fac,
+                                         penalty=ns is not None), engine="grid")
+        assert got == want, (seed, src, dst)
+        if want is not None:
+            arcs, pops, roi_n, phases = ops.stats.cpu().tolist()
+            assert (arcs, pops, roi_n) == (st["scanned"], st["settled"], N)
+            assert phases >= 1
+
+
+def test_full_grid_search_large_lattice():
+    """A 300x200x8 lattice (480k nodes): frontiers spread over every CTA."""
+    g, s, ops, ref = make(300, 200, 8)
+    rng = np.random.default_rng(77)
+    costs = _costs(3, g.E, rng)
+    s.total_cost.copy_(torch.from_numpy(costs))
+    ident = np.arange(g.N, dtype=np.int32)
+    for src, dst in [(5, ref.plane - 7), (int(rng.integers(0, ref.plane)), int(rng.integers(0, ref.plane)))]:
+        st = {}
+        want = find_path_roi_c(ref.indptr, ref.indices, src, dst, costs, ident, ident, stats=st)
+        ops.stats.zero_()
+        got = ops.find_path(ops.net_args(0, src, dst, full_graph=True, penalty=False), engine="grid")
+        assert got == want
+        assert ops.stats.cpu().tolist()[:2] == [st["scanned"], st["settled"]]
+
+
+def test_full_grid_search_unreachable_and_trivial():
+    g, s, ops, ref = make(40, 30, 4)
+    costs = np.full(g.E, np.float32("inf"), dtype=np.float32)
+    s.total_cost.copy_(torch.from_numpy(costs))
+    assert ops.find_path(ops.net_args(0, 3, 100, full_graph=True, penalty=False), engine="grid") is None
+    s.total_cost.fill_(0.4)
+    assert ops.find_path(ops.net_args(0, 3, 3, full_graph=True, penalty=False), engine="grid") is None
 
 
 def test_find_path_replays_reference_net_trace():

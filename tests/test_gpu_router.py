@@ -30,10 +30,10 @@ def flat(paths):
     return np.asarray(out, dtype=np.int64)
 
 
-def gpu_router(nx, ny, nz, iters, mode="persistent"):
+def gpu_router(nx, ny, nz, iters, mode="persistent", full_engine="grid"):
     from orthoroute_gb300 import Lattice
     from orthoroute_gb300.router import PathFinderConfig, PathFinderRouter
-    R = PathFinderRouter(PathFinderConfig(max_iterations=iters), mode=mode)
+    R = PathFinderRouter(PathFinderConfig(max_iterations=iters), mode=mode, full_engine=full_engine)
     R.initialize_lattice(Lattice(nx, ny, nz), board_bounds(nx, ny))
     return R
 
@@ -68,13 +68,17 @@ def seeded_nets(nx, ny, n, seed, dmin=5, dmax=80):
     return out
 
 
+CASES = [((40, 36, 6), 60, 8, 7, 160, "grid"), ((48, 40, 8), 90, 10, 11, 160, "grid"),
+         ((140, 40, 6), 40, 6, 5, 160, "grid"), ((140, 40, 6), 40, 6, 5, 160, "cta"),
+         ((260, 60, 8), 50, 6, 3, 300, "grid")]
+
+
 @pytest.mark.parametrize("mode", ["persistent", "plain"])
-@pytest.mark.parametrize("dims,n_nets,iters,seed", [((40, 36, 6), 60, 8, 7), ((48, 40, 8), 90, 10, 11),
-                                                    ((140, 40, 6), 40, 6, 5)])
-def test_gpu_router_matches_oracle_loop(dims, n_nets, iters, seed, mode):
+@pytest.mark.parametrize("dims,n_nets,iters,seed,dmax,engine", CASES)
+def test_gpu_router_matches_oracle_loop(dims, n_nets, iters, seed, dmax, engine, mode):
     nx, ny, nz = dims
-    reqs = seeded_nets(nx, ny, n_nets, seed, dmin=5, dmax=160)
-    R = gpu_router(nx, ny, nz, iters, mode)
+    reqs = seeded_nets(nx, ny, n_nets, seed, dmin=5, dmax=dmax)
+    R = gpu_router(nx, ny, nz, iters, mode, engine)
     R.trace = []
     res = R.route_multiple_nets(reqs)
     O = OracleRouter(LatticeSpec(nx, ny, nz), board_bounds(nx, ny), Config(max_iterations=iters), fast=True)
