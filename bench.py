@@ -36,8 +36,23 @@ CONFIGS = {
     # BASELINE configs[0]: 100x100x6, 200 two-pin nets on layer 0, length 5-80, 10 iterations
     "c0": dict(nx=100, ny=100, nz=6, nets=200, iters=10, seed=1234, clusters=False),
     # BASELINE configs[1]: 600x400x12, 2,000 nets, 30% from two 20x20 clusters, <= 40 iterations
-    "c1": dict(nx=600, ny=400, nz=12, nets=2000, iters=40, seed=4321, clusters=True),
+    "c1": dict(nx=600, ny=400, nz=12, nets=2000, iters=40, seed=4321, clusters=True, via_span=4),
 }
+
+
+def via_spans(cfg):
+    """allowed_via_spans of the lattice: every layer pair with |dz| <= via_span
+    (the reference's span, unified_pathfinder.py:1872), or None = all pairs."""
+    k = cfg.get("via_span")
+    if k is None:
+        return None
+    nz = cfg["nz"]
+    return [(a, b) for a in range(nz) for b in range(a + 1, nz) if b - a <= k]
+
+
+def make_lattice(cfg):
+    from orthoroute_gb300 import Lattice
+    return Lattice(cfg["nx"], cfg["ny"], cfg["nz"], allowed_via_spans=via_spans(cfg))
 
 
 def make_requests(cfg):
@@ -138,7 +153,7 @@ def run_ours(args, cfg, rank, world):
         return router.route_multiple_nets(reqs)
 
     router = PathFinderRouter(PathFinderConfig(max_iterations=cfg["iters"]), mode=args.mode)
-    router.initialize_lattice(Lattice(nx, ny, nz), bounds)
+    router.initialize_lattice(make_lattice(cfg), bounds)
     for _ in range(args.warmup):
         job(router)
     dist = world > 1
@@ -167,7 +182,7 @@ def run_ours(args, cfg, rank, world):
         torch.cuda.synchronize()
         t1 = time.perf_counter()
         r2 = PathFinderRouter(PathFinderConfig(max_iterations=cfg["iters"]), mode=args.mode)
-        r2.initialize_lattice(Lattice(nx, ny, nz), bounds)
+        r2.initialize_lattice(make_lattice(cfg), bounds)
         res2 = r2.route_multiple_nets(reqs)
         _ = {k: list(v) for k, v in res2["paths"].items()}
         torch.cuda.synchronize()
@@ -176,7 +191,7 @@ def run_ours(args, cfg, rank, world):
     plain = None
     if args.mode == "persistent" and args.compare_plain:
         rp = PathFinderRouter(PathFinderConfig(max_iterations=cfg["iters"]), mode="plain")
-        rp.initialize_lattice(Lattice(nx, ny, nz), bounds)
+        rp.initialize_lattice(make_lattice(cfg), bounds)
         rp.initialize_state()
         torch.cuda.synchronize()
         t2 = time.perf_counter()
@@ -241,7 +256,8 @@ def cpu_job_sample(cfg, budget_s=20.0):
     tasks = {n: (s, d) for n, s, d in reqs}
     nx, ny, nz = cfg["nx"], cfg["ny"], cfg["nz"]
     t0 = time.perf_counter()
-    R = OracleRouter(LatticeSpec(nx, ny, nz), board_bounds(nx, ny), Config(max_iterations=cfg["iters"]), fast=True)
+    R = OracleRouter(LatticeSpec(nx, ny, nz, allowed_via_spans=via_spans(cfg)), board_bounds(nx, ny),
+                     Config(max_iterations=cfg["iters"]), fast=True)
     if cfg["nets"] <= 400:
         res = R.route(tasks)
         dt = time.perf_counter() - t0

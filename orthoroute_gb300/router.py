@@ -402,8 +402,8 @@ class PathFinderRouter:
         self.layer_bias = np.ones(self.nz, dtype=np.float32)
         self._layer_bias_ema = None
         self.net_paths = {}
-        self.net_to_edges: Dict[str, List[int]] = {}
-        self.edge_to_nets = defaultdict(set)
+        self.net_to_edges: Dict[str, np.ndarray] = {}
+        self._eidx = None
         self.net_id_map: Dict[str, int] = {}
         dev = self.g.device
         self._d_col_pres = torch.zeros((L.nx, L.ny), dtype=torch.float32, device=dev)
@@ -439,7 +439,7 @@ class PathFinderRouter:
         self._layer_bias_ema = None
         self.net_paths = {}
         self.net_to_edges = {}
-        self.edge_to_nets = defaultdict(set)
+        self._eidx = None
         self.net_id_map = {}
         self.iteration = 0
         self._reset_policy_state()
@@ -493,15 +493,20 @@ class PathFinderRouter:
         return x, y, z
 
     def _via_nodes(self, path):
-        nodes = set()
-        for u, v in zip(path, path[1:]):
-            zu, ru = divmod(int(u), self.plane)
-            zv, rv = divmod(int(v), self.plane)
-            if ru != rv or zu == zv:
-                continue
-            for z in range(min(zu, zv), max(zu, zv) + 1):
-                nodes.add(z * self.plane + ru)
-        return sorted(nodes)
+        """Sorted nodes spanned by the via hops of a path (every layer of each barrel)."""
+        a = np.asarray(path, dtype=np.int64)
+        if a.size < 2:
+            return []
+        z, r = np.divmod(a, self.plane)
+        m = (r[:-1] == r[1:]) & (z[:-1] != z[1:])
+        if not m.any():
+            return []
+        lo = np.minimum(z[:-1], z[1:])[m]
+        cnt = np.maximum(z[:-1], z[1:])[m] - lo + 1
+        rr = r[:-1][m]
+        rep = np.repeat(np.arange(cnt.size), cnt)
+        off = np.arange(int(cnt.sum())) - np.repeat(np.cumsum(cnt) - cnt, cnt)
+        return np.unique((lo[rep] + off) * self.plane + rr[rep]).tolist()
 
     def _overused(self):
         """(arc ids, over values) of every arc with present > capacity (device compaction)."""
@@ -565,16 +570,45 @@ class PathFinderRouter:
         self.s.node_history[d] = torch.from_numpy(self.node_history[nodes]).to(self.g.device)
 
     def _update_tracking(self, name, edges):
-        self._clear_tracking(name)
-        self.net_to_edges[name] = edges
-        for e in edges:
-            self.edge_to_nets[e].add(name)
+        self.net_to_edges.pop(name, None)
+        self.net_to_edges[name] = np.asarray(edges, dtype=np.int64)
+        self._eidx = None
 
     def _clear_tracking(self, name):
-        if name in self.net_to_edges:
-            for e in self.net_to_edges[name]:
-                self.edge_to_nets[e].discard(name)
-            del self.net_to_edges[name]
+        if self.net_to_edges.pop(name, None) is not None:
+            self._eidx = None
+
+    def _edge_index(self):
+        """Flat (arc, net) view of net_to_edges, rebuilt after any change:
+        (net names, arcs concatenated in net order, net position per arc)."""
+        if self._eidx is None:
+            names = [n for n, e in self.net_to_edges.items() if len(e)]
+            if names:
+                arrs = [self.net_to_edges[n] for n in names]
+                lens = np.fromiter((a.size for a in arrs), dtype=np.int64, count=len(arrs))
+                flat = np.concatenate(arrs)
+                owner = np.repeat(np.arange(len(names), dtype=np.int64), lens)
+            else:
+                flat = np.zeros(0, dtype=np.int64)
+                owner = np.zeros(0, dtype=np.int64)
+            self._eidx = (names, flat, owner)
+        return self._eidx
+
+    def _edge_over(self, over_idx, over_val):
+        """For every tracked net: (Σ over values of its arcs in its arc order —
+        the left-to-right float sum of the reference's generator — and whether
+        any of its arcs is in over_idx).  over_idx: sorted arc ids."""
+        names, flat, owner = self._edge_index()
+        k = len(names)
+        if k == 0 or len(over_idx) == 0:
+            return names, np.zeros(k, dtype=np.float64), np.zeros(k, dtype=bool)
+        oi = np.asarray(over_idx, dtype=np.int64)
+        pos = np.minimum(np.searchsorted(oi, flat), oi.size - 1)
+        hit = oi[pos] == flat
+        w = np.where(hit, np.asarray(over_val, dtype=np.float64)[pos], 0.0)
+        sums = np.bincount(owner, weights=w, minlength=k)
+        anyhit = np.bincount(owner, weights=hit.astype(np.float64), minlength=k) > 0
+        return names, sums, anyhit
 
     # ------------------------------------------------------------- tallies
     def _compute_overuse(self):
@@ -738,16 +772,15 @@ class PathFinderRouter:
         return edges
 
     def _order_nets(self, tasks):
-        over_map, _, _ = self._over_map()
+        _, over_idx, over_val = self._over_map()
+        names, sums, _ = self._edge_over(over_idx, over_val)
+        cong_of = {n: float(sums[i]) / max(1, self.net_to_edges[n].size) for i, n in enumerate(names)}
         scores = []
         for name, (s, d) in tasks.items():
             sx, sy, sz = self.idx_to_coord(s)
             dx, dy, dz = self.idx_to_coord(d)
             dist = abs(dx - sx) + abs(dy - sy) + abs(dz - sz)
-            cong = 0.0
-            if name in self.net_to_edges:
-                edges = self.net_to_edges[name]
-                cong = sum(float(over_map.get(e, 0.0)) for e in edges) / max(1, len(edges))
+            cong = cong_of.get(name, 0.0)
             scores.append((dist * 3 * (cong + 1), name))
         owners, victims = self.barrel_owner_nets, self.barrel_victim_nets
         scores.sort(key=lambda it: (2 if it[1] in owners and it[1] not in victims else 1 if it[1] in owners else 0,
@@ -855,7 +888,7 @@ class PathFinderRouter:
             n = int(lengths[order[k]])
             if not (status[k] & 1) and n >= 2:
                 path = rows[k, :n].tolist()
-                edges = arow[k, :2 * (n - 1)].tolist()
+                edges = arow[k, :2 * (n - 1)].astype(np.int64)
                 self._mark_nodes(name, path, +1)
                 self.net_paths[name] = path
                 self._update_tracking(name, edges)
@@ -884,26 +917,7 @@ class PathFinderRouter:
         if col_over is None and seg_over is None:
             self._via_pool_keepers, self._via_pool_member_state, self._via_pool_keeper_stagnation = {}, {}, {}
             return set()
-        members = defaultdict(set)
-        for name, path in self.net_paths.items():
-            if not path or len(path) < 2:
-                continue
-            res = set()
-            for u, v in zip(path, path[1:]):
-                xu, yu, zu = self.idx_to_coord(u)
-                xv, yv, zv = self.idx_to_coord(v)
-                if xu != xv or yu != yv or zu == zv:
-                    continue
-                if col_over is not None and col_over[xu, yu]:
-                    res.add(("col", xu, yu))
-                if seg_over is not None:
-                    zl = max(1, min(min(zu, zv), self.nz - 2))
-                    zh = max(1, min(max(zu, zv), self.nz - 2))
-                    for z in range(zl, zh):
-                        if 0 <= z - 1 < P.segZ and seg_over[xu, yu, z - 1]:
-                            res.add(("seg", xu, yu, z - 1))
-            for r in res:
-                members[r].add(name)
+        members = self._via_pool_members(col_over, seg_over)
         rotation_allowed = P.spatial_overuse() <= self._via_keeper_threshold()
         nk, nm, ns, off = {}, {}, {}, set()
         for r, mem in sorted(members.items()):
@@ -932,6 +946,47 @@ class PathFinderRouter:
                 off.update(mem)
         self._via_pool_keepers, self._via_pool_member_state, self._via_pool_keeper_stagnation = nk, nm, ns
         return off
+
+    def _via_pool_members(self, col_over, seg_over):
+        """Nets whose via hops use an over-full via column ("col", x, y) or a
+        via segment ("seg", x, y, z-1) of z in [clamp(zlo), clamp(zhi))."""
+        P = self.pools
+        names = [n for n, p in self.net_paths.items() if p and len(p) >= 2]
+        members = defaultdict(set)
+        if not names:
+            return members
+        arrs = [np.asarray(self.net_paths[n], dtype=np.int64) for n in names]
+        lens = np.fromiter((a.size for a in arrs), dtype=np.int64, count=len(arrs))
+        flat = np.concatenate(arrs)
+        owner = np.repeat(np.arange(len(names), dtype=np.int64), lens)
+        z, r = np.divmod(flat, self.plane)
+        hop = (owner[:-1] == owner[1:]) & (r[:-1] == r[1:]) & (z[:-1] != z[1:])
+        if not hop.any():
+            return members
+        ru = r[:-1][hop]
+        net = owner[:-1][hop]
+        zu, zv = z[:-1][hop], z[1:][hop]
+        y, x = np.divmod(ru, self.nx)
+        pairs = set()
+        if col_over is not None:
+            m = col_over[x, y]
+            for xx, yy, nn in zip(x[m].tolist(), y[m].tolist(), net[m].tolist()):
+                pairs.add((("col", xx, yy), nn))
+        if seg_over is not None:
+            zl = np.clip(np.minimum(zu, zv), 1, self.nz - 2)
+            zh = np.clip(np.maximum(zu, zv), 1, self.nz - 2)
+            cnt = np.maximum(zh - zl, 0)
+            if cnt.sum() > 0:
+                rep = np.repeat(np.arange(cnt.size), cnt)
+                zz = zl[rep] + (np.arange(int(cnt.sum())) - np.repeat(np.cumsum(cnt) - cnt, cnt)) - 1
+                ok = (zz >= 0) & (zz < P.segZ)
+                xs, ys, ns, zz = x[rep][ok], y[rep][ok], net[rep][ok], zz[ok]
+                m = seg_over[xs, ys, zz]
+                for xx, yy, z1, nn in zip(xs[m].tolist(), ys[m].tolist(), zz[m].tolist(), ns[m].tolist()):
+                    pairs.add((("seg", xx, yy, z1), nn))
+        for res, nn in pairs:
+            members[res].add(names[nn])
+        return members
 
     def _effective_cap(self, t):
         cfg = self.config
@@ -968,7 +1023,7 @@ class PathFinderRouter:
         return set(sorted(off, key=lambda n: (-int(self.physical_scores.get(n, 0)), str(n)))[:cap])
 
     def _build_hotset(self, tasks, ripped):
-        over_map, over_idx_arr, _ = self._over_map()
+        over_map, over_idx_arr, over_val_arr = self._over_map()
         over_idx = set(over_idx_arr.tolist())
         via_off = self._find_via_pool_offenders()
         pscores = {n: int(s) for n, s in self.path_node_scores.items() if n in tasks and int(s) > 0}
@@ -986,9 +1041,9 @@ class PathFinderRouter:
                                               random.Random(42 + self.iteration)))
             self._last_hotset_size = len(hot)
             return hot
-        offenders = set()
-        for e in over_idx:
-            offenders.update(self.edge_to_nets.get(e, set()))
+        enames, esums, ehit = self._edge_over(over_idx_arr, over_val_arr)
+        over_sum_of = {n: float(esums[i]) for i, n in enumerate(enames) if ehit[i]}
+        offenders = set(over_sum_of)
         offenders.update(poff)
         for n in tasks:
             self._net_clean_iters[n] = 0 if n in offenders else self._net_clean_iters.get(n, 0) + 1
@@ -1000,7 +1055,7 @@ class PathFinderRouter:
         for n in offenders:
             imp = float(pscores.get(n, 0))
             if n in self.net_to_edges:
-                imp += sum(float(over_map[e]) for e in self.net_to_edges[n] if e in over_idx)
+                imp += over_sum_of.get(n, 0)
             scores.append((imp, n))
         for n in unrouted:
             if n not in offenders:
@@ -1035,7 +1090,7 @@ class PathFinderRouter:
         self.owner.fill(-1)
         self.members = {}
         self.net_to_edges.clear()
-        self.edge_to_nets.clear()
+        self._eidx = None
         if self.store is not None:
             self.store.length.zero_()
         for n, p in self.net_paths.items():
@@ -1049,21 +1104,22 @@ class PathFinderRouter:
         self.pools.rebuild(list(self.net_paths.values()), self.plane, self.nx)
 
     def _rip_top_k(self, k=20):
-        over_map, over_idx_arr, _ = self._over_map()
-        canon = [int(e) for e in over_idx_arr.tolist() if self._arc_is_canonical(int(e))]
-        over_idx = set(canon)
+        over_map, over_idx_arr, over_val_arr = self._over_map()
+        keep = np.asarray([self._arc_is_canonical(int(e)) for e in over_idx_arr.tolist()], dtype=bool)
+        enames, esums, ehit = self._edge_over(over_idx_arr[keep] if keep.size else over_idx_arr,
+                                              over_val_arr[keep] if keep.size else over_val_arr)
+        over_sum_of = {n: float(esums[i]) for i, n in enumerate(enames) if ehit[i]}
         _, _, mscores = self._path_node_conflicts()
         self.path_node_scores = dict(mscores)
         cands = set(mscores)
-        for e in over_idx:
-            cands.update(self.edge_to_nets.get(e, ()))
+        cands.update(over_sum_of)
         scores = []
         for n in cands:
             if not self.net_paths.get(n):
                 continue
             imp = float(mscores.get(n, 0))
             if n in self.net_to_edges:
-                imp += sum(float(over_map[e]) for e in self.net_to_edges[n] if e in over_idx)
+                imp += over_sum_of.get(n, 0)
             if imp > 0:
                 scores.append((imp, n))
         scores.sort(key=lambda it: (-it[0], str(it[1])))
@@ -1420,9 +1476,10 @@ class PathFinderRouter:
         best_state = self._capture()
         unrouted0 = sum(1 for n in tasks if not self.net_paths.get(n))
         best = (unrouted0, int(initial_overuse), int(self.barrel_count))
-        over_map, _, _ = self._over_map()
-        cn = {n for n in self.net_paths if self.net_paths[n]
-              and any(e in over_map for e in self.net_to_edges.get(n, ()))}
+        _, over_idx_arr, over_val_arr = self._over_map()
+        enames, _, ehit = self._edge_over(over_idx_arr, over_val_arr)
+        hit_nets = {n for i, n in enumerate(enames) if ehit[i]}
+        cn = {n for n in self.net_paths if self.net_paths[n] and n in hit_nets}
         cn = self._detail_conflict_nets(cn)
         if not cn:
             return {'success': False}
