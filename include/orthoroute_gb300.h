@@ -202,6 +202,18 @@ int ogr_find_path(const ogr_graph* g, const ogr_state* st, const ogr_net_args* n
                   void* workspace, size_t workspace_bytes, int32_t* path_out,
                   int32_t path_cap, int32_t* path_len_out, int64_t* stats, void* stream);
 
+/* The reference's solver seam, SimpleDijkstra.find_path_roi(src, dst, costs,
+ * roi_nodes, global_to_roi, node_penalty) (unified_pathfinder.py:2451-2548):
+ * search the given ROI (device int32[n_roi], global ids; its order is the
+ * heap's tie order) with arc costs `costs` (device float32[E]) and the
+ * ROI-local node penalty roi_penalty (device float32[n_roi], or NULL).
+ * Duplicate ROI entries are not allowed.  Same outputs, statistics and
+ * status codes as ogr_find_path; synchronises. */
+int ogr_find_path_roi(const ogr_graph* g, const float* costs, const int32_t* roi_nodes, int32_t n_roi,
+                      const float* roi_penalty, int32_t src, int32_t dst, void* workspace,
+                      size_t workspace_bytes, int32_t* path_out, int32_t path_cap,
+                      int32_t* path_len_out, int64_t* stats, void* stream);
+
 /* Commit (sign=+1) or rip up (sign=-1) a path given as device node ids:
  * present +-1 (floored at 0), live-present refresh of those arcs when
  * live != 0, path-node use +-1, barrel ownership of every node spanned by a

@@ -386,7 +386,7 @@ __device__ void roi_build(Shared& sh, const ogr_graph& g, const ogr_net_args& a,
 // src first) to path_out and its length to sh.len, or a status to sh.status.
 __device__ void sssp_roi(Shared& sh, const ogr_graph& g, const ogr_state& st, const ogr_net_args& a, const Ws& w,
                          const int32_t* roi, int32_t R, int32_t* path_out, int32_t path_cap,
-                         unsigned long long* stats_acc, StageClock& clk) {
+                         unsigned long long* stats_acc, StageClock& clk, const float* roi_pen = nullptr) {
   const int tid = threadIdx.x;
   const int lane = tid & 31, warp = tid >> 5;
   const int sl = tid & (kSub - 1), grp = tid / kSub;
@@ -497,7 +497,8 @@ __device__ void sssp_roi(Shared& sh, const ogr_graph& g, const ogr_state& st, co
         float p = 0.0f;
         if (valid) {
           fresh = node[y].st == ST_NONE;
-          if (sl == 0) p = fresh ? ogr_node_penalty(st, a, full ? y : roi[y]) : node[y].pen;
+          if (sl == 0)
+            p = !fresh ? node[y].pen : (roi_pen ? roi_pen[y] : ogr_node_penalty(st, a, full ? y : roi[y]));
         }
         p = __shfl_sync(0xffffffffu, p, lane & 16);
         const double pd = (double)p;
@@ -783,6 +784,27 @@ find_path_kernel(ogr_graph g, ogr_state st, ogr_net_args a, Ws w, int32_t* path_
   }
 }
 
+// The reference's solver seam: search a given ROI (ROI order = tie order)
+// with a given ROI-local penalty array (or none).
+__global__ void __launch_bounds__(kThreads, 1)
+find_path_given_roi_kernel(ogr_graph g, ogr_state st, ogr_net_args a, Ws w, const int32_t* roi, int32_t R,
+                           const float* roi_pen, int32_t* path_out, int32_t path_cap, int64_t* stats) {
+  __shared__ Shared sh;
+  StageClock clk;
+  clk.start();
+  if (threadIdx.x == 0) {
+    sh.status = OGR_OK;
+    sh.len = 0;
+    sh.found = 0;
+  }
+  __syncthreads();
+  sssp_roi(sh, g, st, a, w, roi, R, path_out, path_cap, reinterpret_cast<unsigned long long*>(stats), clk, roi_pen);
+  if (threadIdx.x == 0) {
+    w.result[0] = sh.status;
+    w.result[1] = sh.len;
+  }
+}
+
 __global__ void __launch_bounds__(kThreads, 1)
 roi_kernel(ogr_graph g, ogr_net_args a, Ws w, int32_t* roi_out, int32_t roi_cap) {
   __shared__ Shared sh;
@@ -1057,6 +1079,37 @@ extern "C" int ogr_find_path(const ogr_graph* g, const ogr_state* st, const ogr_
   ws_layout(g->num_nodes, (char*)ws, &w);
   cudaStream_t s = ogr_stream(stream);
   find_path_kernel<<<1, kThreads, 0, s>>>(*g, *st, *net, w, path_out, path_cap, stats);
+  OGR_LAUNCH_CHECK();
+  int64_t res[2];
+  OGR_CUDA_TRY(cudaMemcpyAsync(res, w.result, sizeof(res), cudaMemcpyDeviceToHost, s));
+  OGR_CUDA_TRY(cudaStreamSynchronize(s));
+  *path_len_out = (res[0] == OGR_OK) ? (int32_t)res[1] : 0;
+  return (int)res[0];
+}
+
+extern "C" int ogr_find_path_roi(const ogr_graph* g, const float* costs, const int32_t* roi_nodes, int32_t n_roi,
+                                 const float* roi_penalty, int32_t src, int32_t dst, void* ws, size_t bytes,
+                                 int32_t* path_out, int32_t path_cap, int32_t* path_len_out, int64_t* stats,
+                                 void* stream) {
+  if (!g || !costs || !roi_nodes || !ws || !path_out || !path_len_out || n_roi < 0 || n_roi > g->num_nodes)
+    return OGR_ERR_ARG;
+  if (bytes < ogr_route_workspace_bytes(g->num_nodes)) return OGR_ERR_CAPACITY;
+  if (src < 0 || dst < 0 || src >= g->num_nodes || dst >= g->num_nodes) return OGR_ERR_ARG;
+  *path_len_out = 0;
+  if (n_roi == 0) return OGR_NO_PATH;
+  Ws w;
+  ws_layout(g->num_nodes, (char*)ws, &w);
+  ogr_state st{};
+  st.total_cost = const_cast<float*>(costs);
+  ogr_net_args a{};
+  a.net_id = -1;
+  a.src = src;
+  a.dst = dst;
+  a.full_graph = 0;
+  a.penalty_enabled = 0;
+  cudaStream_t s = ogr_stream(stream);
+  find_path_given_roi_kernel<<<1, kThreads, 0, s>>>(*g, st, a, w, roi_nodes, n_roi, roi_penalty, path_out, path_cap,
+                                                    stats);
   OGR_LAUNCH_CHECK();
   int64_t res[2];
   OGR_CUDA_TRY(cudaMemcpyAsync(res, w.result, sizeof(res), cudaMemcpyDeviceToHost, s));

@@ -234,6 +234,24 @@ class Ops:
             return None
         return self.path_buf[: n.value].cpu().tolist()
 
+    def find_path_given_roi(self, src: int, dst: int, costs: torch.Tensor, roi_nodes, roi_penalty=None,
+                            slot: int = 0) -> Optional[List[int]]:
+        """``SimpleDijkstra.find_path_roi`` seam: search a caller-given ROI with
+        caller-given arc costs (device f32[E]) and ROI-local penalties."""
+        dev = self.g.device
+        roi = torch.as_tensor(np.asarray(roi_nodes, dtype=np.int32)).to(dev)
+        pen = None if roi_penalty is None else torch.as_tensor(np.asarray(roi_penalty, dtype=np.float32)).to(dev)
+        g = self.g.cgraph()
+        n = C.c_int32(0)
+        rc = self.lib.ogr_find_path_roi(C.byref(g), _p(costs), _p(roi), int(roi.numel()), _p(pen), int(src),
+                                        int(dst), _p(self.ws[slot]), self.ws_bytes, _p(self.path_buf),
+                                        int(self.path_buf.numel()), C.byref(n), _p(self.stats), self._sp())
+        _lib.check(rc, "ogr_find_path_roi")
+        self.counters["launches"] += 1
+        if rc == _lib.OGR_NO_PATH or n.value < 2:
+            return None
+        return self.path_buf[: n.value].cpu().tolist()
+
     def extract_roi(self, net: _lib.NetArgs, slot: int = 0) -> np.ndarray:
         g = self.g.cgraph()
         out = torch.empty(self.g.N, dtype=torch.int32, device=self.g.device)
@@ -343,7 +361,13 @@ def route_pass(ops: "Ops", store: PathStore, table: dict, order: np.ndarray, *, 
     ops._ev1.synchronize()
     ops.counters["search_ms"] += ops._ev0.elapsed_time(ops._ev1)
     ops.counters["search_launches"] += 1
-    ops.counters["launches"] += 1
+    n_launch = 1 if rb is not None else 0
+    if full_flags is None:
+        n_launch += 1
+    else:
+        runs = int(np.count_nonzero((full_flags[1:] == 0) & (full_flags[:-1] != 0))) + int(full_flags[0] == 0)
+        n_launch += runs + 3 * int(np.count_nonzero(full_flags))
+    ops.counters["launches"] += n_launch
     ops.counters["h2d_bytes"] += 4 * k
     ops.counters["d2h_bytes"] += 4 * k + 32
     return status[:k].cpu().numpy(), stats.cpu().numpy()

@@ -334,6 +334,40 @@ def test_find_path_replays_reference_net_trace():
         np.testing.assert_array_equal(np.asarray(got or [], dtype=np.int32), z[f"r0_t{j}_path"])
 
 
+def test_solver_seam_replays_reference_net_trace():
+    """ogr_find_path_roi with the reference's own ROI, costs and penalty arrays."""
+    meta = json.load(open(os.path.join(G, "golden.json")))["r0"]
+    g, s, ops, ref = make(meta["nx"], meta["ny"], meta["nz"])
+    z = np.load(os.path.join(G, "runs.npz"))
+    for j in range(meta["n_trace"]):
+        src, dst = z[f"r0_t{j}_sd"].tolist()
+        costs = torch.from_numpy(z[f"r0_t{j}_costs"]).to(g.device)
+        pen = z[f"r0_t{j}_pen"] if f"r0_t{j}_pen" in z else None
+        ops.stats.zero_()
+        got = ops.find_path_given_roi(src, dst, costs, z[f"r0_t{j}_roi"], pen)
+        np.testing.assert_array_equal(np.asarray(got or [], dtype=np.int32), z[f"r0_t{j}_path"])
+
+
+@pytest.mark.parametrize("seed", range(3))
+def test_solver_seam_matches_oracle(seed):
+    g, s, ops, ref = make(48, 40, 6)
+    rng = np.random.default_rng(50 + seed)
+    costs = _costs(seed % 4, g.E, rng)
+    d_costs = torch.from_numpy(costs).to(g.device)
+    for _ in range(4):
+        src, dst = (int(v) for v in rng.integers(0, ref.plane, size=2))
+        r = roi_radius(src, dst, ref.nx, ref.plane)
+        roi, g2r = extract_roi_bfs(ref.indptr, ref.indices, g.N, src, dst, initial_radius=r)
+        pen = (rng.integers(0, 3, size=len(roi)) * rng.random(len(roi))).astype(np.float32)
+        st = {}
+        want = find_path_roi(ref.indptr, ref.indices, src, dst, costs, roi, g2r, node_penalty=pen, stats=st)
+        ops.stats.zero_()
+        got = ops.find_path_given_roi(src, dst, d_costs, roi, pen)
+        assert got == want
+        if want is not None:
+            assert ops.stats.cpu().tolist()[:3] == [st["scanned"], st["settled"], len(roi)]
+
+
 def test_apply_path_node_state_matches_oracle():
     g, s, ops, ref = make(20, 16, 8)
     ns = NodeState(g.N, ref.nx, ref.plane)
