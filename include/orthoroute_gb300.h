@@ -92,6 +92,11 @@ int ogr_costs_update(const ogr_cost_args* a, float* total_cost, void* stream);
 int ogr_live_begin(const ogr_cost_args* a, const float* present, float* total_cost,
                    float* live_static, void* stream);
 
+/* rcost[e] = total_cost[rev[e]]: the cost of the arc into each CSR row's
+ * node, read by the searches in row order (no counterpart in the reference). */
+int ogr_reverse_costs(int64_t num_edges, const int32_t* rev, const float* total_cost, float* rcost,
+                      void* stream);
+
 /* update_present_ema (unified_pathfinder.py:1291-1299). */
 int ogr_present_ema(int64_t num_edges, const float* present, float* present_ema,
                     float beta, float one_minus_beta, void* stream);
@@ -170,6 +175,10 @@ typedef struct {
   int32_t* owner_count;        /* barrel ownership: #nets per node            */
   int32_t* owner_xor;          /* XOR of those net ids (= id when count==1)   */
   const float* node_history;
+  float* rcost;                /* NULL, or rcost[e] = total_cost[rev[e]] kept in
+                                  sync by ogr_path_apply / ogr_route_pass; after
+                                  any other change of total_cost call
+                                  ogr_reverse_costs before the next search     */
 } ogr_state;
 
 typedef struct {
@@ -306,8 +315,9 @@ int ogr_route_pass(const ogr_graph* g, const ogr_state* st, const ogr_net_table*
  * 8219-8262, into find_path_roi :2451-2548 with roi_nodes = all nodes).  Same
  * result, statistics and status codes as ogr_find_path with
  * net->full_graph = 1, computed by one cooperative launch on all SMs.  The
- * workspace (about 44 bytes per node + 4 per arc) is initialised once with
- * ogr_full_workspace_init; searches then touch only the nodes they reach.
+ * workspace (about 36 bytes per node + 4 per arc) is initialised once with
+ * ogr_full_workspace_init; a search rewrites the 8-byte key word of every
+ * node and otherwise touches only the nodes it reaches.
  * OGR_ERR_TIMEOUT: a grid barrier gave up (not expected; the launch is
  * sized so every CTA is resident).  Synchronises. */
 size_t ogr_full_workspace_bytes(int32_t num_nodes, int64_t num_edges);

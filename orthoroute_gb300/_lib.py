@@ -26,7 +26,7 @@ EXPORTED = [
     "ogr_find_path", "ogr_path_apply", "ogr_extract_roi", "ogr_via_pools_apply", "ogr_overused_arcs",
     "ogr_find_path_noalloc", "ogr_route_pass", "ogr_search_profile", "ogr_bfs_workspace_bytes",
     "ogr_bfs_workspace_init", "ogr_full_workspace_bytes", "ogr_find_path_full",
-    "ogr_full_profile", "ogr_full_workspace_init", "ogr_find_path_roi",
+    "ogr_full_profile", "ogr_full_workspace_init", "ogr_find_path_roi", "ogr_reverse_costs",
 ]
 
 P = C.c_void_p
@@ -56,7 +56,7 @@ class Graph(C.Structure):
 class State(C.Structure):
     _fields_ = [("total_cost", P), ("live_static", P), ("present", P), ("capacity", P), ("layer_bias", P),
                 ("edge_layer", P), ("edge_kind", P), ("path_node_use", P), ("owner_count", P),
-                ("owner_xor", P), ("node_history", P)]
+                ("owner_xor", P), ("node_history", P), ("rcost", P)]
 
 
 class NetArgs(C.Structure):
@@ -126,6 +126,7 @@ def load(build_if_missing: bool = True):
         "ogr_full_workspace_bytes": [I32, I64],
         "ogr_find_path_roi": [C.POINTER(Graph), P, P, I32, P, I32, I32, P, C.c_size_t, P, I32, C.POINTER(I32), P, P],
         "ogr_full_profile": [P, I32],
+        "ogr_reverse_costs": [I64, P, P, P, P],
         "ogr_full_workspace_init": [P, C.c_size_t, I32, I64, P],
         "ogr_find_path_full": [C.POINTER(Graph), C.POINTER(State), C.POINTER(NetArgs), P, C.c_size_t, P, I32,
                                C.POINTER(I32), P, P],

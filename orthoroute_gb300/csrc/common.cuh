@@ -28,15 +28,18 @@ __device__ __forceinline__ unsigned long long ogr_dbits(double d) {
 
 // Node penalty of the search (_build_owner_penalty, unified_pathfinder.py:
 // 5308-5384): foreign barrel owner + occupied path node + history, float32.
+// The four loads are unconditional so they issue together.
 __device__ __forceinline__ float ogr_node_penalty(const ogr_state& st, const ogr_net_args& a, int32_t gid) {
   if (!a.penalty_enabled) return 0.0f;
   const int32_t cnt = st.owner_count[gid];
-  const int32_t owner = (cnt == 0) ? -1 : (cnt == 1 ? st.owner_xor[gid] : -2);
+  const int32_t xr = st.owner_xor[gid];
+  const int32_t use = st.path_node_use[gid];
+  const float hist = st.node_history[gid];
+  const int32_t owner = (cnt == 0) ? -1 : (cnt == 1 ? xr : -2);
   const bool foreign = (owner != -1) && (owner != a.net_id);
-  const bool occupied = st.path_node_use[gid] > 0;
   const float f = foreign ? a.owner_weight : 0.0f;
-  const float o = occupied ? a.path_weight : 0.0f;
-  return __fadd_rn(__fadd_rn(f, o), __fmul_rn(st.node_history[gid], a.history_weight));
+  const float o = use > 0 ? a.path_weight : 0.0f;
+  return __fadd_rn(__fadd_rn(f, o), __fmul_rn(hist, a.history_weight));
 }
 
 // (a32, lu, u) lexicographic less-than.

@@ -131,6 +131,21 @@ __global__ void tally_kernel(int64_t E, int32_t N, int32_t nz, const float* __re
 
 }  // namespace
 
+__global__ void reverse_cost_kernel(int64_t E, const int32_t* __restrict__ rev, const float* __restrict__ total,
+                                    float* __restrict__ rcost) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < E; e += stride) rcost[e] = total[rev[e]];
+}
+
+extern "C" int ogr_reverse_costs(int64_t E, const int32_t* rev, const float* total_cost, float* rcost,
+                                 void* stream) {
+  if (E < 0 || (E > 0 && (!rev || !total_cost || !rcost))) return OGR_ERR_ARG;
+  if (E == 0) return OGR_OK;
+  reverse_cost_kernel<<<ogr_blocks(E, 256), 256, 0, ogr_stream(stream)>>>(E, rev, total_cost, rcost);
+  OGR_LAUNCH_CHECK();
+  return OGR_OK;
+}
+
 extern "C" int ogr_costs_update(const ogr_cost_args* a, float* total_cost, void* stream) {
   if (!a || !total_cost || a->num_edges < 0) return OGR_ERR_ARG;
   cost_kernel<<<ogr_blocks(a->num_edges, kThreads, 152 * 32), kThreads, 0, ogr_stream(stream)>>>(*a, total_cost);

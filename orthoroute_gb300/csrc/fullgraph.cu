@@ -3,31 +3,29 @@
 // The reference searches nets whose Manhattan length is 125 steps or more on
 // the full graph (_route_all, unified_pathfinder.py:8219-8262: roi_nodes =
 // arange(N)), so its heap Dijkstra (find_path_roi, :2451-2548) settles every
-// node cheaper than dst — most of a 600x400x12 lattice.  This kernel computes
-// the same result as the per-CTA search in route.cu (each node takes the
-// lexicographic minimum of (float32(alt), L(u), u) over its settled
-// in-neighbours; nodes are settled in phases by the IN-criterion) with the
-// node states in global memory and all SMs working on each phase.
+// node cheaper than dst — most of a 600x400x12 lattice.  The result here is
+// the same as the heap's: every node takes the lexicographic minimum of
+// (float32(alt), L(u), u) over its in-neighbours u, alt = (L(u) + c) + pen.
 //
-// One phase = two grid-wide steps:
-//   E  every node settled last phase claims its unsettled out-neighbours
-//      (atomicMax on a per-node stamp: one claimer per node and phase) and
-//      the claimer's 16-lane group recomputes the claimed node from all its
-//      settled in-neighbours; newly reached nodes join the frontier;
-//   S  with T = the smallest frontier label, frontier nodes with label == T
-//      or float32 key < float32((T + cin) + pen) are settled.
-// T is the minimum of the labels written in E and of the labels carried over
-// in the previous S.  Recomputing a node can move its FP64 label within the
-// same float32 value in either direction, so T may lie below the true
-// minimum; both settling tests only get stricter then (no label equals such
-// a T, and the IN bound is monotone in T), the phase settles a subset of what
-// it would have, and the next phase's T is exact again.  The result is a
-// function of the settled set alone, independent of thread scheduling.
+// Phases, one grid step each.  Every frontier node v pulls its key, label
+// and parent from the in-neighbours settled before this phase (settle-phase
+// stamps make that set a snapshot) and cin(v), its cheapest in-arc from any
+// other node.  With T = a lower bound of the frontier's labels, v is final
+// when L(v) == T or key(v) < float32((T + cin) + pen) — the IN criterion.  A
+// node that settles marks its unreached out-neighbours as reached (they join
+// the next frontier) and offers its candidate labels to the next T.  Every
+// decision of a phase depends only on the set settled before it, so the
+// result does not depend on thread timing.  T for the next phase is the
+// minimum of the labels carried over and of the settling nodes' candidate
+// labels; a label recomputed from a new winner can move within one float32
+// value in either direction, so T may lie below the true minimum, which only
+// makes both tests stricter.
 //
 // The kernel is launched cooperatively with one grid of fully resident CTAs
-// (occupancy API), and its grid barrier gives up after a bounded wait and
-// reports OGR_ERR_TIMEOUT.  List appends are staged per CTA in shared memory
-// and published with one global atomic per CTA and list.
+// (occupancy API); its grid barrier gives up after a bounded wait and reports
+// OGR_ERR_TIMEOUT.  Per-node words carry the search's phase numbers (reach
+// stamp, settle stamp), which keep increasing across searches, so no search
+// clears per-node memory.  List appends are staged per CTA in shared memory.
 #include <cooperative_groups.h>
 
 #include "fullgraph.cuh"
@@ -37,44 +35,41 @@ namespace cg = cooperative_groups;
 namespace {
 
 constexpr int kThreads = 512;
-constexpr int kSub = 8;                    // lanes per recomputed node
+constexpr int kSub = 16;                   // lanes per examined node
 constexpr int kGroups = kThreads / kSub;   // groups per CTA
-constexpr int32_t ST_FRONT = 1, ST_DONE = 2;   // state 0 (or another epoch): unreached
-constexpr int kStage = 1536;               // staged list entries per CTA and list
-constexpr int kClaim = 3072;               // claimed nodes per CTA and phase held in shared memory
+constexpr int kStage = 2048;               // staged list entries per CTA and list
 constexpr unsigned kBarSpin = 1u << 22;
-constexpr int32_t kMaxEpoch = (1 << 29) - 1;
-
-// Node state.  `st` = (epoch << 2) | state: a node whose epoch is not the
-// current search's is unreached, so a search clears no per-node memory.
-// `stamp` = global phase number of the last claim (monotone across searches).
-struct __align__(32) FNode {
-  double lab;
-  float m32;
-  float pen;
-  float cin;
-  int32_t par;
-  int32_t st;
-  int32_t stamp;
-};
-static_assert(sizeof(FNode) == 32, "FNode must fill one 32-byte sector");
 
 struct FCtl {
   alignas(128) unsigned long long bar_count;   // monotone arrival counter
   alignas(128) int32_t bar_err;
-  alignas(128) unsigned long long tbits[2];
-  alignas(128) int32_t nfront[2];
+  alignas(128) unsigned long long tbits[3];
+  alignas(128) int32_t nfront[3];
   alignas(128) int32_t nlog;                   // settled-log length
   alignas(128) int32_t res[4];
-  int32_t epoch;                               // persistent across searches
-  int32_t gbase;
+  int32_t gbase;                               // persistent across searches
 };
 
+// Per-node search record: label, settle stamp, reach stamp in one 16-byte
+// load.  A reader uses lab only where sp says the node settled in an earlier
+// phase (written before the barrier), so a record torn by a concurrent settle
+// of this phase is never misread.
+struct __align__(16) NodeRec {
+  double lab;        // label, valid once settled in this search
+  int32_t sp;        // phase number of the settle (this search: > gbase)
+  int32_t reach;     // == gbase: reached in this search
+};
+
+// Frontier entry: node, its CSR row [f0, f1) and its penalty bits, filled in
+// by whoever appends it, so the examination starts with the row.
+using FEntry = int4;
+
 struct FWs {
-  FNode* node;
-  float* rcost;   // rcost[e] = cost of the arc opposite to e, i.e. into the row's node
-  int32_t* fr[2];
-  int32_t* log;   // settled nodes in settle order
+  NodeRec* rec;
+  int32_t* par;              // winning in-neighbour, valid once settled
+  float* rcost;              // reverse-arc cost gather when the state carries none
+  FEntry* fr[3];             // frontier lists: read, write, and the one being cleared
+  int32_t* log;              // settled nodes in settle order
   FCtl* ctl;
 };
 
@@ -90,19 +85,18 @@ size_t fws_layout(int32_t N, int64_t E, char* base, FWs* w) {
   const size_t n = (size_t)N;
   FWs t{};
   t.ctl = (FCtl*)take(sizeof(FCtl));
-  t.node = (FNode*)take(32 * n);
+  t.rec = (NodeRec*)take(16 * n);
+  t.par = (int32_t*)take(4 * n);
   t.rcost = (float*)take(4 * (size_t)E);
-  t.fr[0] = (int32_t*)take(4 * n);
-  t.fr[1] = (int32_t*)take(4 * n);
+  for (int i = 0; i < 3; ++i) t.fr[i] = (FEntry*)take(16 * n);
   t.log = (int32_t*)take(4 * n);
   if (w) *w = t;
   return off;
 }
 
 struct Smem {
-  int32_t buf[2][kStage];
-  int32_t claim[kClaim];
-  int32_t nclaim;
+  FEntry fbuf[kStage];
+  int32_t lbuf[kStage];
   int32_t cnt[2];
   int32_t base[2];
   unsigned long long tmin;
@@ -124,14 +118,14 @@ __device__ __forceinline__ unsigned long long gtimer() {
 }
 
 // Tracing counters of the whole-lattice search (read with ogr_full_profile):
-// [0] searches, [1] phases, [2] kernel ns, [3] init ns (CTA 0), [4] work ns
-// of the E steps and [5] of the S steps (largest CTA total), [6] barrier
+// [0] searches, [1] phases, [2] kernel ns, [3] init ns (CTA 0), [4] phase
+// work ns (largest CTA total), [5] frontier entries examined, [6] barrier
 // wait ns (CTA 0), [7] statistics + backtrace ns (CTA 0).
 __device__ unsigned long long g_full_prof[8];
 
 // Per-CTA timing kept by thread 0.
 struct Clock {
-  unsigned long long mark, init, e, s, wait;
+  unsigned long long mark, init, e, wait;
 };
 
 // Grid barrier on a monotone arrival counter: the k-th barrier of a launch
@@ -164,99 +158,67 @@ __device__ bool grid_barrier(FCtl* c, unsigned long long& target, Smem& sm, Cloc
   return sm.flag != 0;
 }
 
-__device__ __forceinline__ void stage_push(Smem& sm, int k, int32_t v, int32_t* gl, int32_t* gcnt) {
-  const int i = atomicAdd(&sm.cnt[k], 1);
-  if (i < kStage)
-    sm.buf[k][i] = v;
-  else
-    gl[atomicAdd(gcnt, 1)] = v;
-}
-
-// Publishes lists 0..nl-1 of this CTA (call after __syncthreads, from all
-// threads): one global reservation per list, then a coalesced copy.
-__device__ __forceinline__ void stage_flush(Smem& sm, int nl, int32_t* gl0, int32_t* gc0, int32_t* gl1,
-                                            int32_t* gc1) {
-  if (threadIdx.x == 0) {
-    for (int k = 0; k < nl; ++k) {
-      const int n = min(sm.cnt[k], kStage);
-      sm.base[k] = n ? atomicAdd(k == 0 ? gc0 : gc1, n) : 0;
-      sm.cnt[k] = n;
+// Appends x to the staged frontier list (k = 0) or the settled log (k = 1)
+// from the lanes of `tile` whose `want` is set: one shared-memory
+// reservation per tile; past the staging capacity the entry goes straight to
+// the global list.
+template <typename Tile, typename T>
+__device__ __forceinline__ void stage_push_tile(Tile& tile, Smem& sm, int k, bool want, const T& x, T* gl,
+                                                int32_t* gcnt) {
+  const unsigned m = tile.ballot(want);
+  if (m == 0) return;
+  const int lead = __ffs(m) - 1;
+  int base = 0;
+  if ((int)tile.thread_rank() == lead) base = atomicAdd(&sm.cnt[k], __popc(m));
+  base = tile.shfl(base, lead);
+  if (want) {
+    const int i = base + __popc(m & ((1u << tile.thread_rank()) - 1u));
+    if (i < kStage) {
+      if constexpr (sizeof(T) == sizeof(FEntry))
+        sm.fbuf[i] = x;
+      else
+        sm.lbuf[i] = x;
+    } else {
+      gl[atomicAdd(gcnt, 1)] = x;
     }
   }
-  __syncthreads();
-  for (int k = 0; k < nl; ++k) {
-    const int n = sm.cnt[k], b = sm.base[k];
-    int32_t* gl = k == 0 ? gl0 : gl1;
-    for (int i = threadIdx.x; i < n; i += kThreads) gl[b + i] = sm.buf[k][i];
+}
+
+// Publishes both staged lists of this CTA (call after __syncthreads, from all
+// threads): one global reservation per list, issued together, then a
+// coalesced copy.
+__device__ __forceinline__ void stage_flush(Smem& sm, FEntry* gf, int32_t* gfc, int32_t* gl, int32_t* glc) {
+  if (threadIdx.x == 0) {
+    const int n0 = min(sm.cnt[0], kStage), n1 = min(sm.cnt[1], kStage);
+    const int b0 = n0 ? atomicAdd(gfc, n0) : 0;
+    const int b1 = n1 ? atomicAdd(glc, n1) : 0;
+    sm.cnt[0] = n0;
+    sm.cnt[1] = n1;
+    sm.base[0] = b0;
+    sm.base[1] = b1;
   }
+  __syncthreads();
+  const int n0 = sm.cnt[0], b0 = sm.base[0], n1 = sm.cnt[1], b1 = sm.base[1];
+  for (int i = threadIdx.x; i < n0; i += kThreads) gf[b0 + i] = sm.fbuf[i];
+  for (int i = threadIdx.x; i < n1; i += kThreads) gl[b1 + i] = sm.lbuf[i];
 }
 
 __device__ __forceinline__ void stage_reset(Smem& sm) {
   if (threadIdx.x == 0) {
     sm.cnt[0] = 0;
     sm.cnt[1] = 0;
-    sm.nclaim = 0;
     sm.tmin = ~0ull;
   }
   __syncthreads();
 }
 
-// Recomputes node yy from all its settled in-neighbours with W lanes (lane
-// `sl` of the tile; W = 1 runs on one thread without shuffles).  A node
-// reached for the first time gets its penalty and joins the frontier list.
-template <int W, typename Tile>
-__device__ __forceinline__ void recompute(Tile& tile, int sl, int32_t yy, int32_t ep2, const ogr_graph& g,
-                                          const ogr_state& st, const ogr_net_args& a, const FWs& w, Smem& sm,
-                                          int32_t* fr, int32_t* nfront) {
-  const float kInf = __int_as_float(0x7f800000);
-  const int32_t* __restrict__ indptr = g.indptr;
-  const int32_t* __restrict__ indices = g.indices;
-  FNode* __restrict__ node = w.node;
-  FNode* ny = &node[yy];
-  const bool fresh = (__ldcg(&ny->st) & ~3) != ep2;
-  const float p = fresh ? ogr_node_penalty(st, a, yy) : __ldcg(&ny->pen);
-  const double pd = (double)p;
-  float ba = kInf, bc = kInf, cin = kInf;
-  double bl = 0.0;
-  int32_t bu = 0x7fffffff;
-  const int32_t f1 = indptr[yy + 1];
-  for (int32_t f = indptr[yy] + sl; f < f1; f += W) {
-    const int32_t u = indices[f];
-    const float c = w.rcost[f];
-    const int32_t su = __ldcg(&node[u].st);
-    const double lu = __ldcg(&node[u].lab);
-    if (su != (ep2 | ST_DONE)) {
-      cin = fminf(cin, c);
-      continue;
-    }
-    const float a32 = __double2float_rn((lu + (double)c) + pd);
-    if (!(a32 < kInf)) continue;
-    if (ogr_key_lt(a32, lu, u, ba, bl, bu)) { ba = a32; bl = lu; bu = u; bc = c; }
-  }
-#pragma unroll
-  for (int o = W / 2; o > 0; o >>= 1) {
-    const float oa = tile.shfl_xor(ba, o);
-    const double ol = tile.shfl_xor(bl, o);
-    const int32_t ou = tile.shfl_xor(bu, o);
-    const float oc = tile.shfl_xor(bc, o);
-    if (ogr_key_lt(oa, ol, ou, ba, bl, bu)) { ba = oa; bl = ol; bu = ou; bc = oc; }
-    cin = fminf(cin, tile.shfl_xor(cin, o));
-  }
-  if (sl == 0) {
-    if (fresh) ny->pen = p;
-    ny->cin = cin;
-    if (ba < kInf) {
-      const double lab = (bl + (double)bc) + pd;
-      ny->m32 = ba;
-      ny->lab = lab;
-      ny->par = bu;
-      atomicMin(&sm.tmin, ogr_dbits(lab));
-      if (fresh) {
-        ny->st = ep2 | ST_FRONT;
-        stage_push(sm, 0, yy, fr, nfront);
-      }
-    }
-  }
+__device__ __forceinline__ NodeRec ld_rec(const NodeRec* p) {
+  const int4 q = __ldcg(reinterpret_cast<const int4*>(p));
+  NodeRec r;
+  r.lab = __hiloint2double(q.y, q.x);
+  r.sp = q.z;
+  r.reach = q.w;
+  return r;
 }
 
 __global__ void __launch_bounds__(kThreads, 2)
@@ -295,7 +257,8 @@ full_sssp_kernel(ogr_graph g, ogr_state st, ogr_full::Job job, FWs w) {
   }
   const int32_t* __restrict__ indptr = g.indptr;
   const int32_t* __restrict__ indices = g.indices;
-  FNode* __restrict__ node = w.node;
+  const float* __restrict__ fcost = st.total_cost;
+  NodeRec* __restrict__ rec = w.rec;
   const float kInf = __int_as_float(0x7f800000);
   auto tile = cg::tiled_partition<kSub>(cg::this_thread_block());
   Clock clk{};
@@ -305,42 +268,38 @@ full_sssp_kernel(ogr_graph g, ogr_state st, ogr_full::Job job, FWs w) {
     clk.mark = t_start;
   }
   unsigned long long bar_target = 0;
+  unsigned long long examined = 0;
 
-  // Epoch and phase numbering; when either would run out of range every node
-  // is reset (all CTAs read the same persistent words, so all decide alike).
-  int32_t ep = __ldcg(&ctl->epoch) + 1;
+  // Phase numbers continue across searches, so the stamps of older searches
+  // (<= gbase) read as unreached / unsettled; when they would run out of range
+  // the stamps are cleared (all CTAs read the same persistent word).
   int32_t gbase = __ldcg(&ctl->gbase);
   const int max_phase = 2 * N + 4;
-  if (ep < 1 || ep > kMaxEpoch || gbase < 1 || gbase > 0x7fffffff - (max_phase + 8)) {
+  if (gbase < 1 || gbase > 0x7fffffff - (max_phase + 8)) {
     for (int64_t r = gtid; r < N; r += gthreads)
-      if (r != src) *reinterpret_cast<int2*>(&node[r].st) = make_int2(0, 0);   // src is written below
-    ep = 1;
+      if (r != src) {
+        rec[r].sp = 0;
+        rec[r].reach = 0;
+      }
     gbase = 1;
   }
-  const int32_t ep2 = ep << 2;
-  {
+  const float* rc = st.rcost;
+  if (rc == nullptr) {
     const int32_t* __restrict__ rev = g.rev;
-    const float* __restrict__ tc = st.total_cost;
-    float* __restrict__ rc = w.rcost;
+    float* __restrict__ out = w.rcost;
 #pragma unroll 4
-    for (int64_t e = gtid; e < E; e += gthreads) rc[e] = tc[rev[e]];
+    for (int64_t e = gtid; e < E; e += gthreads) out[e] = fcost[rev[e]];
+    rc = w.rcost;
   }
   if (leader) {
-    FNode s0;
-    s0.lab = 0.0;
-    s0.m32 = 0.0f;
-    s0.pen = 0.0f;
-    s0.cin = kInf;
-    s0.par = -1;
-    s0.st = ep2 | ST_DONE;
-    s0.stamp = gbase;
-    node[src] = s0;
-    ctl->nfront[0] = 0;
-    ctl->nfront[1] = 0;
-    ctl->nlog = 1;
-    ctl->tbits[0] = ~0ull;
-    ctl->tbits[1] = ~0ull;
-    w.log[0] = src;
+    rec[src].reach = gbase;
+    rec[src].sp = 0;
+    w.fr[0][0] = make_int4(src, indptr[src], indptr[src + 1], __float_as_int(0.0f));
+    for (int i = 0; i < 3; ++i) {
+      ctl->nfront[i] = i == 0 ? 1 : 0;
+      ctl->tbits[i] = i == 0 ? 0ull : ~0ull;   // T of phase 0 = L(src) = 0
+    }
+    ctl->nlog = 0;
   }
   bool alive = grid_barrier(ctl, bar_target, sm, clk, &clk.init);
   int status = OGR_OK;
@@ -351,46 +310,11 @@ full_sssp_kernel(ogr_graph g, ogr_state st, ogr_full::Job job, FWs w) {
   const bool want_stats = job.stats != nullptr;
   bool dst_done = false;
   double ld = 0.0;
-  int32_t lo = 0, hi = 1;   // log range settled in the previous phase
   int phase = 0;
   while (alive) {
-    const int q = phase & 1;
+    const int b = phase % 3, bn = (phase + 1) % 3, bz = (phase + 2) % 3;
     const int32_t gp = gbase + 1 + phase;
-    stage_reset(sm);
-    if (leader) {
-      ctl->nfront[q ^ 1] = 0;
-      ctl->tbits[q ^ 1] = ~0ull;
-    }
-    // E: the nodes settled last phase, dealt round-robin over the CTAs,
-    // claim their unsettled out-neighbours; then the CTA's groups recompute
-    // the claimed nodes from the shared-memory list.
-    {
-      for (int64_t i = lo + blockIdx.x + (int64_t)gi * nblocks; i < hi; i += (int64_t)nblocks * kGroups) {
-        const int32_t x = __ldcg(&w.log[i]);
-        const int32_t e1 = indptr[x + 1];
-        for (int32_t e = indptr[x] + sl; e < e1; e += kSub) {
-          const int32_t y = indices[e];
-          const int32_t sy = __ldcg(&node[y].st);
-          if (atomicMax(&node[y].stamp, gp) < gp && sy != (ep2 | ST_DONE)) {
-            const int j = atomicAdd(&sm.nclaim, 1);
-            if (j < kClaim)
-              sm.claim[j] = y;
-            else
-              recompute<1>(tile, 0, y, ep2, g, st, a, w, sm, w.fr[q], &ctl->nfront[q]);
-          }
-        }
-      }
-      __syncthreads();
-      const int nc = min(sm.nclaim, kClaim);
-      for (int j = gi; j < nc; j += kGroups)
-        recompute<kSub>(tile, sl, sm.claim[j], ep2, g, st, a, w, sm, w.fr[q], &ctl->nfront[q]);
-      __syncthreads();
-      stage_flush(sm, 1, w.fr[q], &ctl->nfront[q], nullptr, nullptr);
-      if (tid == 0 && sm.tmin != ~0ull) atomicMin(&ctl->tbits[q], sm.tmin);
-    }
-    alive = grid_barrier(ctl, bar_target, sm, clk, &clk.e);
-    if (!alive) break;
-    const int nf = __ldcg(&ctl->nfront[q]);
+    const int nf = __ldcg(&ctl->nfront[b]);
     if (nf == 0) {
       if (dst_done)
         found = true;
@@ -398,45 +322,125 @@ full_sssp_kernel(ogr_graph g, ogr_state st, ogr_full::Job job, FWs w) {
         status = OGR_NO_PATH;
       break;
     }
-    const double T = __longlong_as_double((long long)__ldcg(&ctl->tbits[q]));
+    const double T = __longlong_as_double((long long)__ldcg(&ctl->tbits[b]));
     if (dst_done && T > ld) {
       found = true;
       break;
     }
-    // S: settle every frontier node whose state can no longer change
-    {
-      stage_reset(sm);
-      const int32_t* fr = w.fr[q];
-      for (int64_t i = blockIdx.x + (int64_t)tid * nblocks; i < nf; i += gthreads) {
-        const int32_t x = __ldcg(&fr[i]);
-        FNode* nx = &node[x];
-        const double lab = __ldcg(&nx->lab);
-        const float m32 = __ldcg(&nx->m32);
-        const float cin = __ldcg(&nx->cin);
-        const float pen = __ldcg(&nx->pen);
-        const bool settle = (lab == T) || m32 < __double2float_rn((T + (double)cin) + (double)pen);
-        if (settle) {
-          nx->st = ep2 | ST_DONE;
-          stage_push(sm, 1, x, w.log, &ctl->nlog);
-        } else {
-          stage_push(sm, 0, x, w.fr[q ^ 1], &ctl->nfront[q ^ 1]);
-          atomicMin(&sm.tmin, ogr_dbits(lab));
-        }
-      }
-      __syncthreads();
-      stage_flush(sm, 2, w.fr[q ^ 1], &ctl->nfront[q ^ 1], w.log, &ctl->nlog);
-      if (tid == 0 && sm.tmin != ~0ull) atomicMin(&ctl->tbits[q ^ 1], sm.tmin);
+    stage_reset(sm);
+    if (leader) {
+      ctl->nfront[bz] = 0;
+      ctl->tbits[bz] = ~0ull;
     }
-    alive = grid_barrier(ctl, bar_target, sm, clk, &clk.s);
+    const FEntry* fr = w.fr[b];
+    FEntry* frn = w.fr[bn];
+    for (int64_t i = blockIdx.x + (int64_t)gi * nblocks; i < nf; i += (int64_t)nblocks * kGroups) {
+      const FEntry ent = __ldcg(&fr[i]);
+      const int32_t v = ent.x, f0 = ent.y, f1 = ent.z;
+      const float pv = __int_as_float(ent.w);
+      const double pd = (double)pv;
+      const bool is_src = v == src;
+      const bool one_pass = f1 - f0 <= kSub;
+      // pull: the lexicographic minimum of the candidates of the in-neighbours
+      // settled before this phase; cin from the others.  One-pass rows keep
+      // each lane's neighbour data (stamps, penalty, CSR row) for the marking.
+      float ba = kInf, bc = kInf, cin = kInf;
+      double bl = 0.0;
+      int32_t bu = 0x7fffffff;
+      int32_t u0 = -1, s0 = 0, r0 = 0, i0 = 0, i1 = 0;
+      float cout0 = kInf, p0 = 0.0f;
+      for (int32_t f = f0 + sl; f < f1; f += kSub) {
+        const int32_t u = indices[f];
+        const float c = rc[f];
+        const NodeRec ru = ld_rec(&rec[u]);
+        if (one_pass) {
+          u0 = u;
+          s0 = ru.sp;
+          r0 = ru.reach;
+          cout0 = fcost[f];
+          p0 = ogr_node_penalty(st, a, u);
+          i0 = indptr[u];
+          i1 = indptr[u + 1];
+        }
+        if (!(ru.sp > gbase && ru.sp < gp)) {
+          cin = fminf(cin, c);
+          continue;
+        }
+        const float a32 = __double2float_rn((ru.lab + (double)c) + pd);
+        if (!(a32 < kInf)) continue;
+        if (ogr_key_lt(a32, ru.lab, u, ba, bl, bu)) { ba = a32; bl = ru.lab; bu = u; bc = c; }
+      }
+#pragma unroll
+      for (int o = kSub / 2; o > 0; o >>= 1) {
+        const float oa = tile.shfl_xor(ba, o);
+        const double ol = tile.shfl_xor(bl, o);
+        const int32_t ou = tile.shfl_xor(bu, o);
+        const float oc = tile.shfl_xor(bc, o);
+        if (ogr_key_lt(oa, ol, ou, ba, bl, bu)) { ba = oa; bl = ol; bu = ou; bc = oc; }
+        cin = fminf(cin, tile.shfl_xor(cin, o));
+      }
+      const double lv = is_src ? 0.0 : (bl + (double)bc) + pd;
+      const float m32 = is_src ? 0.0f : ba;
+      const bool settle = (lv == T) || m32 < __double2float_rn((T + (double)cin) + pd);
+      examined += (sl == 0);
+      if (!settle) {
+        stage_push_tile(tile, sm, 0, sl == 0, ent, frn, &ctl->nfront[bn]);
+        if (sl == 0) atomicMin(&sm.tmin, ogr_dbits(lv));
+        continue;
+      }
+      if (sl == 0) {
+        rec[v].lab = lv;
+        rec[v].sp = gp;
+        w.par[v] = is_src ? -1 : bu;
+      }
+      stage_push_tile(tile, sm, 1, sl == 0, v, w.log, &ctl->nlog);
+      // mark the unreached out-neighbours and offer the candidate labels
+      unsigned long long tl = ~0ull;
+      for (int32_t fb = f0; fb < f1; fb += kSub) {   // same trip count on every lane (ballots inside)
+        const int32_t f = fb + sl;
+        const bool act = f < f1;
+        int32_t y = -1, sy = 0;
+        if (act) {
+          y = one_pass ? u0 : indices[f];
+          sy = one_pass ? s0 : __ldcg(&rec[y].sp);
+        }
+        bool fresh = false;
+        FEntry ny = make_int4(0, 0, 0, 0);
+        if (act && !(sy > gbase)) {   // settled nodes cannot improve
+          const float c = one_pass ? cout0 : fcost[f];
+          const float py = one_pass ? p0 : ogr_node_penalty(st, a, y);
+          const double ly = (lv + (double)c) + (double)py;
+          if (__double2float_rn(ly) < kInf) {
+            const unsigned long long bits = ogr_dbits(ly);
+            tl = bits < tl ? bits : tl;
+            const int32_t ry = one_pass ? r0 : __ldcg(&rec[y].reach);
+            fresh = ry != gbase && atomicExch(&rec[y].reach, gbase) != gbase;
+            if (fresh) ny = make_int4(y, one_pass ? i0 : indptr[y], one_pass ? i1 : indptr[y + 1], __float_as_int(py));
+          }
+        }
+        stage_push_tile(tile, sm, 0, fresh, ny, frn, &ctl->nfront[bn]);
+      }
+#pragma unroll
+      for (int o = kSub / 2; o > 0; o >>= 1) {
+        const unsigned long long ot = tile.shfl_xor(tl, o);
+        tl = ot < tl ? ot : tl;
+      }
+      if (sl == 0 && tl != ~0ull) atomicMin(&sm.tmin, tl);
+    }
+    __syncthreads();
+    stage_flush(sm, frn, &ctl->nfront[bn], w.log, &ctl->nlog);
+    if (tid == 0 && sm.tmin != ~0ull) atomicMin(&ctl->tbits[bn], sm.tmin);
+    alive = grid_barrier(ctl, bar_target, sm, clk, &clk.e);
     if (!alive) break;
-    lo = hi;
-    hi = __ldcg(&ctl->nlog);
-    if (!dst_done && __ldcg(&node[dst].st) == (ep2 | ST_DONE)) {
-      dst_done = true;
-      ld = __ldcg(&node[dst].lab);
-      if (!want_stats) {
-        found = true;
-        break;
+    if (!dst_done) {
+      const NodeRec rd = ld_rec(&rec[dst]);
+      if (rd.sp > gbase) {
+        dst_done = true;
+        ld = rd.lab;
+        if (!want_stats) {
+          found = true;
+          break;
+        }
       }
     }
     if (++phase > max_phase) {
@@ -445,13 +449,14 @@ full_sssp_kernel(ogr_graph g, ogr_state st, ogr_full::Job job, FWs w) {
     }
   }
   if (!alive) status = OGR_ERR_TIMEOUT;
+  const int nlog = __ldcg(&ctl->nlog);
   // statistics: the rows of every node the sequential search pops before dst
   // (all of them are in the settled log)
   if (found && want_stats) {
     unsigned long long arcs = 0, pops = 0;
-    for (int64_t i = gtid; i < hi; i += gthreads) {
+    for (int64_t i = gtid; i < nlog; i += gthreads) {
       const int32_t r = __ldcg(&w.log[i]);
-      const double lr = __ldcg(&node[r].lab);
+      const double lr = __ldcg(&rec[r].lab);
       if (lr < ld || (lr == ld && r < dst)) {
         arcs += (unsigned long long)(indptr[r + 1] - indptr[r]);
         ++pops;
@@ -472,10 +477,9 @@ full_sssp_kernel(ogr_graph g, ogr_state st, ogr_full::Job job, FWs w) {
       atomicAdd(&job.stats[3], (unsigned long long)(phase + 1));
     }
   }
-  if (tid == 0) {
-    atomicMax(&g_full_prof[4], clk.e);
-    atomicMax(&g_full_prof[5], clk.s);
-  }
+  if (tid == 0) atomicMax(&g_full_prof[4], clk.e);
+  examined = __reduce_add_sync(0xffffffffu, (unsigned)examined);
+  if (lane == 0 && examined) atomicAdd(&g_full_prof[5], examined);
   if (blockIdx.x != 0) return;
   // backtrace dst -> src in one walk (reversed into path_out), then CTA 0
   // turns it around
@@ -486,7 +490,7 @@ full_sssp_kernel(ogr_graph g, ogr_state st, ogr_full::Job job, FWs w) {
       int32_t c = dst;
       while (c != -1 && len < limit) {
         path_out[len++] = c;
-        c = __ldcg(&node[c].par);
+        c = __ldcg(&w.par[c]);
       }
       if (c != -1) status = len >= N ? OGR_ERR_ITER_CAP : OGR_ERR_CAPACITY;
       else if (len < 2) status = OGR_NO_PATH;
@@ -507,7 +511,6 @@ full_sssp_kernel(ogr_graph g, ogr_state st, ogr_full::Job job, FWs w) {
   ctl->res[0] = status;
   ctl->res[1] = len;
   ctl->res[2] = phase + 1;
-  ctl->epoch = ep;
   ctl->gbase = gbase + phase + 2;
   const unsigned long long t_end = gtimer();
   atomicAdd(&g_full_prof[0], 1ull);
@@ -572,7 +575,7 @@ extern "C" int ogr_full_workspace_init(void* ws, size_t bytes, int32_t num_nodes
   if (bytes < ogr_full::workspace_bytes(num_nodes, num_edges)) return OGR_ERR_CAPACITY;
   FWs w;
   fws_layout(num_nodes, num_edges, (char*)ws, &w);
-  // epoch 0 / phase base 0: the first search resets every node
+  // phase base 0: the first search clears the settle stamps
   OGR_CUDA_TRY(cudaMemsetAsync(w.ctl, 0, sizeof(FCtl), ogr_stream(stream)));
   return OGR_OK;
 }

@@ -424,7 +424,7 @@ __device__ void sssp_roi(Shared& sh, const ogr_graph& g, const ogr_state& st, co
         float c = kInf;
         if (e < e1) {
           u = w.g2r[indices[e]];
-          c = st.total_cost[g.rev[e]];
+          c = st.rcost ? st.rcost[e] : st.total_cost[g.rev[e]];
         }
         w.adj[(int64_t)r * kDMax + k] = u;
         w.acost[(int64_t)r * kDMax + k] = c;
@@ -529,7 +529,7 @@ __device__ void sssp_roi(Shared& sh, const ogr_graph& g, const ogr_state& st, co
               const int32_t ug = indices[e];
               const int32_t u = full ? ug : w.g2r[ug];
               if (u < 0) continue;
-              const float c = st.total_cost[g.rev[e]];
+              const float c = st.rcost ? st.rcost[e] : st.total_cost[g.rev[e]];
               if (node[u].st != ST_DONE) {
                 cin = fminf(cin, c);
                 continue;
@@ -731,7 +731,9 @@ __device__ int apply_path_dev(const ogr_graph& g, const ogr_state& st, const int
         const float bias = (st.layer_bias != nullptr && st.edge_kind[e] == 0) ? st.layer_bias[st.edge_layer[e]] : 1.0f;
         const float scale = st.layer_bias != nullptr ? __fmul_rn(pres_fac, bias) : pres_fac;
         const float prosp = fmaxf(0.0f, __fsub_rn(__fadd_rn(p, 1.0f), st.capacity[e]));
-        st.total_cost[e] = __fadd_rn(st.live_static[e], __fmul_rn(scale, prosp));
+        const float tc = __fadd_rn(st.live_static[e], __fmul_rn(scale, prosp));
+        st.total_cost[e] = tc;
+        if (st.rcost) st.rcost[k == 0 ? r : f] = tc;   // the opposite arc's row entry
       }
     }
   }

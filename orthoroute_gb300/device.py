@@ -89,12 +89,21 @@ class DeviceState:
         self.owner_count = torch.zeros(N, dtype=torch.int32, device=dev)
         self.owner_xor = torch.zeros(N, dtype=torch.int32, device=dev)
         self.node_history = torch.zeros(N, dtype=torch.float32, device=dev)
+        self.rcost = None   # reverse costs, kept in sync once enabled (see enable_rcost)
+
+    def enable_rcost(self):
+        """Keep rcost[e] = total_cost[rev[e]] in HBM: the searches then read the
+        cost into each row's node directly.  Every writer of total_cost must be
+        followed by Ops.sync_rcost (the path-apply kernels keep it in sync)."""
+        if self.rcost is None:
+            self.rcost = torch.empty_like(self.total_cost)
 
     def cstate(self) -> _lib.State:
         g = self.g
         return _lib.State(_p(self.total_cost), _p(self.live_static), _p(self.present), _p(self.capacity),
                           _p(self.layer_bias) if self.use_layer_bias else None, _p(g.edge_layer), _p(g.edge_kind),
-                          _p(self.path_node_use), _p(self.owner_count), _p(self.owner_xor), _p(self.node_history))
+                          _p(self.path_node_use), _p(self.owner_count), _p(self.owner_xor), _p(self.node_history),
+                          _p(self.rcost))
 
     def cost_args(self, pres_fac, hist_weight, via_mult, base_weight, add_jitter=True) -> _lib.CostArgs:
         g = self.g
@@ -144,6 +153,7 @@ class Ops:
         a = s.cost_args(pres_fac, hist_weight, via_mult, base_weight)
         _lib.check(self.lib.ogr_costs_update(C.byref(a), _p(s.total_cost), self._sp()), "ogr_costs_update")
         self.counters["launches"] += 1
+        self.sync_rcost()
         if layer_bias is not None:
             self.counters["h2d_bytes"] += 4 * len(layer_bias)
 
@@ -152,6 +162,16 @@ class Ops:
         a = s.cost_args(pres_fac, 0.0, 1.0, 1.0)
         _lib.check(self.lib.ogr_live_begin(C.byref(a), _p(s.present), _p(s.total_cost), _p(s.live_static),
                                            self._sp()), "ogr_live_begin")
+        self.counters["launches"] += 1
+        self.sync_rcost()
+
+    def sync_rcost(self):
+        """Re-derive the reverse costs after a full-array change of total_cost."""
+        s, g = self.s, self.g
+        if s.rcost is None:
+            return
+        _lib.check(self.lib.ogr_reverse_costs(g.E, _p(g.rev), _p(s.total_cost), _p(s.rcost), self._sp()),
+                   "ogr_reverse_costs")
         self.counters["launches"] += 1
 
     def present_ema(self, beta=0.40):

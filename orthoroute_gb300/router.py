@@ -386,6 +386,7 @@ class PathFinderRouter:
         self.bounds = bounds
         self.g = DeviceGraph(lattice, device=self.device)
         self.s = DeviceState(self.g)
+        self.s.enable_rcost()
         self.ops = Ops(self.g, self.s)
         L = lattice
         self.nx, self.ny, self.nz = L.nx, L.ny, L.nz
@@ -426,6 +427,8 @@ class PathFinderRouter:
         for t in (s.present, s.present_ema, s.history, s.total_cost, s.live_static, s.path_node_use,
                   s.owner_count, s.owner_xor, s.node_history):
             t.zero_()
+        if s.rcost is not None:
+            s.rcost.zero_()
         s.layer_bias.fill_(1.0)
         s.use_layer_bias = False
         self.pools = _ViaPools(self.nx, self.ny, self.nz)
@@ -722,6 +725,7 @@ class PathFinderRouter:
             self._d_seg_use.data_ptr() if seg else None, self._d_seg_cap.data_ptr() if seg else None,
             self._d_disc.data_ptr(), float(np.float32(1.0)), float(np.float32(1.0)), float(np.float32(pres_fac)),
             int(bool(penalty)), int(bool(block)), self.s.total_cost.data_ptr(), None), "ogr_via_pools_apply")
+        self.ops.sync_rcost()
 
     def _layer_bias_for_costs(self):
         """``_compute_layer_bias`` (:8451-8534) from exact device tallies."""
