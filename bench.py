@@ -8,7 +8,7 @@ resident in HBM; ``e2e`` is the same job through the public router API
 starting from host requests (CSR build, state upload and the path read-back
 inside the timed region).
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--config c0|c1]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--config c1|c0]
                     [--impl ours|reference]
 
 ``--impl reference`` times the CPU restatement of the reference's routing
@@ -39,7 +39,7 @@ CONFIGS = {
     # plain_iters: the plain one-net-per-launch form is compared on the first iteration only
     # searches_per_job: searches of the (bit-identical) job, used to scale the CPU sample
     "c1": dict(nx=600, ny=400, nz=12, nets=2000, iters=40, seed=4321, clusters=True, via_span=4,
-               plain_iters=1, searches_per_job=10364),
+               plain_iters=1, plain_nets=200, searches_per_job=10364),
 }
 
 
@@ -140,6 +140,23 @@ def peaks():
         return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
 
 
+# ----------------------------------------------------------------- replicas
+def replica_max(ms: float, device: str) -> float:
+    """Max over ranks of one replica's time per job (a route job does not
+    shard: every rank routes its own copy, with no exchange on the data path)."""
+    import torch
+    import torch.distributed as tdist
+    t = torch.tensor([float(ms)], dtype=torch.float64, device=device)
+    tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(ms: float, world: int) -> float:
+    """Whole-job throughput of N replicas expressed in the metric's unit
+    (seconds per job): N jobs finish every `ms`."""
+    return ms / 1e3 / max(1, world)
+
+
 # --------------------------------------------------------------------- our arm
 def run_ours(args, cfg, rank, world):
     import torch
@@ -197,13 +214,15 @@ def run_ours(args, cfg, rank, world):
         # plain form: one launch per net, one CTA per search (full-graph nets included), host
         # round trip per net; compared on the whole job, or on its first iterations for c1
         k_it = cfg.get("plain_iters") or cfg["iters"]
+        preqs = reqs[:cfg["plain_nets"]] if cfg.get("plain_nets") else reqs
+        whole = k_it == cfg["iters"] and len(preqs) == len(reqs)
 
         def timed(r, iters):
             r.config = PathFinderConfig(max_iterations=iters)
             r.initialize_state()
             torch.cuda.synchronize()
             t = time.perf_counter()
-            out = r.route_multiple_nets(reqs)
+            out = r.route_multiple_nets(preqs)
             torch.cuda.synchronize()
             return time.perf_counter() - t, out
 
@@ -211,19 +230,17 @@ def run_ours(args, cfg, rank, world):
         rp.initialize_lattice(make_lattice(cfg), bounds)
         t_plain, resp = timed(rp, k_it)
         del rp
-        if k_it == cfg["iters"]:
+        if whole:
             t_batched, resb = None, results[-1]
         else:
             t_batched, resb = timed(router, k_it)
         same = {k: list(v) for k, v in resp["paths"].items()} == {k: list(v) for k, v in resb["paths"].items()}
-        plain = {"iterations": k_it, "plain_s": round(t_plain, 4), "identical_paths": bool(same)}
+        plain = {"iterations": k_it, "nets": len(preqs), "plain_s": round(t_plain, 4), "identical_paths": bool(same)}
         if t_batched is not None:
             plain["batched_s"] = round(t_batched, 4)
     ms = max(dev_ms, wall * 1e3) / args.steps
     if dist:
-        t = torch.tensor([ms], device="cuda")
-        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
-        ms = float(t.item())
+        ms = replica_max(ms, "cuda")
     res = results[-1]
     pk, pk_kind = peaks()
     search_ms = prof["search_kernel_ms"]
@@ -233,7 +250,7 @@ def run_ours(args, cfg, rank, world):
     gteps = prof["arcs"] / (search_ms * 1e-3) / 1e9 if search_ms > 0 else 0.0
     line = {
         "metric": "PathFinder time-to-zero-overuse (s per routing job; capped iterations when not converged)",
-        "value": round(ms / 1e3 / (1 if not dist else 1), 6) if world == 1 else round(ms / 1e3 / world, 6),
+        "value": round(replica_value(ms, world), 6),
         "unit": "s/job",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3),
         "higher_is_better": False, "scaling": "weak" if world > 1 else "weak",
@@ -317,9 +334,9 @@ def run_reference(args, cfg):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=None, help="timed jobs (default: 1 for c1, 3 for c0)")
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--config", default="c0", choices=sorted(CONFIGS))
+    ap.add_argument("--config", default="c1", choices=sorted(CONFIGS))
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--mode", default="persistent", choices=["persistent", "plain"])
@@ -327,6 +344,8 @@ def main():
     ap.add_argument("--no-compare-plain", dest="compare_plain", action="store_false")
     args = ap.parse_args()
     cfg = CONFIGS[args.config]
+    if args.steps is None:
+        args.steps = 1 if args.config == "c1" else 3
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     if args.impl == "reference":
