@@ -293,13 +293,39 @@ typedef struct {
   int32_t* roi_len;
   int32_t roi_cap;
   int32_t* next;
+  int32_t* roi_box;            /* NULL, or [4*num_nets]: x0, x1, y0, y1 of the
+                                  BFS region holding each ROI                   */
 } ogr_roi_batch;
+
+/* Batched disjoint-ROI windows for the ROI nets of a pass.  Consecutive ROI
+ * nets whose footprints (the ROI's box and the box of the net's old path) are
+ * pairwise disjoint are ripped up and searched together, one CTA each, in one
+ * cooperative launch; they then commit in order.  A net whose ROI search
+ * fails ends its window: the later nets' rip-ups are undone and it takes its
+ * fallback in order.  The results are those of the sequential pass.
+ * ws holds `slots` search slots of slot_bytes (ogr_window_workspace_*),
+ * scratch holds slots x slot_cap path nodes, ctl is device scratch of
+ * ogr_window_ctl_bytes(slots) bytes. */
+typedef struct {
+  int32_t slots;
+  size_t slot_bytes;
+  void* ws;
+  int32_t* scratch;
+  void* ctl;
+} ogr_window_args;
+
+size_t ogr_window_workspace_bytes(int32_t num_nodes, int32_t max_roi_nodes, int32_t slots);
+int ogr_window_workspace_init(void* workspace, int32_t num_nodes, int32_t max_roi_nodes, int32_t slots,
+                              void* stream);
+size_t ogr_window_ctl_bytes(int32_t slots);
 
 size_t ogr_bfs_workspace_bytes(int32_t num_nodes, int64_t qcap, int32_t slots);
 int ogr_bfs_workspace_init(void* workspace, int32_t num_nodes, int64_t qcap, int32_t slots,
                            void* stream);
 
-/* rb may be NULL (every ROI is extracted inline, in order).
+/* rb may be NULL (every ROI is extracted inline, in order).  win (may be
+ * NULL) batches the ROI nets into disjoint windows; it needs rb with
+ * roi_box.
  * order_full (HOST uint8[count], may be NULL) marks the entries of `order`
  * that are full-graph nets; each of those is searched by the whole-lattice
  * search (ogr_find_path_full) in full_workspace, the ROI nets between them by
@@ -308,7 +334,8 @@ int ogr_bfs_workspace_init(void* workspace, int32_t num_nodes, int64_t qcap, int
 int ogr_route_pass(const ogr_graph* g, const ogr_state* st, const ogr_net_table* t,
                    const ogr_pass_args* pa, const ogr_roi_batch* rb, void* workspace,
                    size_t workspace_bytes, const uint8_t* order_full, void* full_workspace,
-                   size_t full_workspace_bytes, int32_t* status_out, void* stream);
+                   size_t full_workspace_bytes, const ogr_window_args* win, int32_t* status_out,
+                   void* stream);
 
 /* Whole-lattice search for nets with Manhattan length >= 125 (the
  * reference's full-graph branch of _route_all, unified_pathfinder.py:

@@ -27,6 +27,7 @@ EXPORTED = [
     "ogr_find_path_noalloc", "ogr_route_pass", "ogr_search_profile", "ogr_bfs_workspace_bytes",
     "ogr_bfs_workspace_init", "ogr_full_workspace_bytes", "ogr_find_path_full",
     "ogr_full_profile", "ogr_full_workspace_init", "ogr_find_path_roi", "ogr_reverse_costs",
+    "ogr_window_workspace_bytes", "ogr_window_workspace_init", "ogr_window_ctl_bytes",
 ]
 
 P = C.c_void_p
@@ -80,7 +81,11 @@ class PassArgs(C.Structure):
 
 class RoiBatch(C.Structure):
     _fields_ = [("slots", I32), ("slot_bytes", C.c_size_t), ("qcap", I64), ("bfs_ws", P), ("roi_pool", P),
-                ("roi_len", P), ("roi_cap", I32), ("next", P)]
+                ("roi_len", P), ("roi_cap", I32), ("next", P), ("roi_box", P)]
+
+
+class WindowArgs(C.Structure):
+    _fields_ = [("slots", I32), ("slot_bytes", C.c_size_t), ("ws", P), ("scratch", P), ("ctl", P)]
 
 
 _LIB = None
@@ -122,7 +127,11 @@ def load(build_if_missing: bool = True):
                                   C.POINTER(I32), P, P],
         "ogr_search_profile": [P, I32],
         "ogr_route_pass": [C.POINTER(Graph), C.POINTER(State), C.POINTER(NetTable), C.POINTER(PassArgs),
-                           C.POINTER(RoiBatch), P, C.c_size_t, P, P, C.c_size_t, C.POINTER(I32), P],
+                           C.POINTER(RoiBatch), P, C.c_size_t, P, P, C.c_size_t, C.POINTER(WindowArgs),
+                           C.POINTER(I32), P],
+        "ogr_window_workspace_bytes": [I32, I32, I32],
+        "ogr_window_workspace_init": [P, I32, I32, I32, P],
+        "ogr_window_ctl_bytes": [I32],
         "ogr_full_workspace_bytes": [I32, I64],
         "ogr_find_path_roi": [C.POINTER(Graph), P, P, I32, P, I32, I32, P, C.c_size_t, P, I32, C.POINTER(I32), P, P],
         "ogr_full_profile": [P, I32],

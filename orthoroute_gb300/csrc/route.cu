@@ -113,6 +113,35 @@ __host__ inline size_t ws_layout(int32_t N, char* base, Ws* w) {
   return off;
 }
 
+// A search-only slot for the window pass: the global->ROI map and ROI-sized
+// arrays (the ROI comes from the batched extraction, so no BFS state).
+__host__ __device__ inline size_t ws_slot_layout(int32_t N, int32_t Rmax, char* base, Ws* w) {
+  size_t off = 0;
+  char* p[11];
+  const size_t n = (size_t)N, r = (size_t)Rmax, ad = min_sz(r, kAdjCap);
+  const size_t sz[11] = {4 * n, 32 * r, 4 * r, 4 * r, 4 * r, 4 * r, 4 * ad * kDMax, 4 * ad * kDMax, 4 * ad, 64, 0};
+  for (int i = 0; i < 10; ++i) {
+    p[i] = base ? base + off : nullptr;
+    off += round256(sz[i]);
+  }
+  if (w) {
+    Ws t{};
+    t.g2r = (int32_t*)p[0];
+    t.node = (NodeSt*)p[1];
+    t.fr[0] = (int32_t*)p[2];
+    t.fr[1] = (int32_t*)p[3];
+    t.dl = (int32_t*)p[4];
+    t.blist = (int32_t*)p[5];
+    t.adj = (int32_t*)p[6];
+    t.acost = (float*)p[7];
+    t.deg = (int32_t*)p[8];
+    t.result = (int64_t*)p[9];
+    t.qcap = 0;
+    *w = t;
+  }
+  return off;
+}
+
 // A BFS-only slot for the batched ROI extraction: seen[N] + 4 queues.
 struct BfsSlot {
   int32_t* seen;
@@ -882,7 +911,15 @@ roi_batch_kernel(ogr_graph g, ogr_net_table t, ogr_pass_args pa, ogr_roi_batch r
     if (threadIdx.x == 0) sh.status = OGR_OK;
     __syncthreads();
     roi_build(sh, g, a, slot.seen, slot.q, slot.qcap, rb.roi_pool + (int64_t)n * rb.roi_cap, rb.roi_cap, clk);
-    if (threadIdx.x == 0) rb.roi_len[n] = (sh.status == OGR_OK) ? sh.R : -1;
+    if (threadIdx.x == 0) {
+      rb.roi_len[n] = (sh.status == OGR_OK) ? sh.R : -1;
+      if (rb.roi_box) {
+        rb.roi_box[4 * n + 0] = sh.bx0;
+        rb.roi_box[4 * n + 1] = sh.bx1;
+        rb.roi_box[4 * n + 2] = sh.by0;
+        rb.roi_box[4 * n + 3] = sh.by1;
+      }
+    }
     __syncthreads();
   }
 }
@@ -970,6 +1007,273 @@ route_pass_kernel(ogr_graph g, ogr_state st, ogr_net_table t, ogr_pass_args pa, 
   }
 }
 
+// ---- batched disjoint-ROI windows ---------------------------------------------
+// Control block of the window pass (device scratch, cleared per launch).
+struct WinCtl {
+  unsigned long long bar_count;
+  int32_t bar_err;
+  int32_t cursor;
+  int32_t wsize;
+  int32_t error;
+};
+
+struct WinSlots {
+  int32_t* k;                      // position in the order of the window's b-th net
+  int32_t* solo;                   // 1: ROI extracted inline (the batched one overflowed)
+  int32_t* st;                     // status of the b-th search
+  int32_t* len;                    // path length of the b-th search
+  int32_t* box;                    // [4] footprint box
+  unsigned long long* stats;       // [4] the b-th search's statistics, added on acceptance
+};
+
+__host__ __device__ inline size_t win_ctl_layout(int32_t slots, char* base, WinCtl** c, WinSlots* s) {
+  size_t off = round256(sizeof(WinCtl));
+  const size_t k = (size_t)slots;
+  char* p[6];
+  const size_t sz[6] = {4 * k, 4 * k, 4 * k, 4 * k, 16 * k, 32 * k};
+  for (int i = 0; i < 6; ++i) {
+    p[i] = base ? base + off : nullptr;
+    off += round256(sz[i]);
+  }
+  if (c) *c = (WinCtl*)base;
+  if (s) {
+    s->k = (int32_t*)p[0];
+    s->solo = (int32_t*)p[1];
+    s->st = (int32_t*)p[2];
+    s->len = (int32_t*)p[3];
+    s->box = (int32_t*)p[4];
+    s->stats = (unsigned long long*)p[5];
+  }
+  return off;
+}
+
+constexpr unsigned kWinBarSpin = 1u << 24;
+
+// Bounded grid barrier (monotone arrival counter); false once any CTA gave up.
+__device__ bool win_barrier(WinCtl* c, unsigned long long& target, int* s_flag) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    target += gridDim.x;
+    int ok = 1;
+    asm volatile("fence.acq_rel.gpu;" ::: "memory");
+    asm volatile("red.relaxed.gpu.global.add.u64 [%0], 1;" ::"l"(&c->bar_count) : "memory");
+    unsigned it = 0;
+    while (true) {
+      unsigned long long v;
+      asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(&c->bar_count) : "memory");
+      if (v >= target) break;
+      if (++it > kWinBarSpin || *(volatile int32_t*)&c->bar_err) {
+        atomicExch(&c->bar_err, 1);
+        ok = 0;
+        break;
+      }
+      if (it > 64) __nanosleep(64);
+    }
+    *s_flag = ok;
+  }
+  __syncthreads();
+  return *s_flag != 0;
+}
+
+__device__ __forceinline__ bool boxes_meet(const int* a, const int* b) {
+  return !(a[1] < b[0] || b[1] < a[0] || a[3] < b[2] || b[3] < a[2]);
+}
+
+// Copies a path found into scratch to the net's store slot and commits it.
+__device__ int commit_from(const ogr_graph& g, const ogr_state& st, const ogr_net_table& t, const ogr_pass_args& pa,
+                           int32_t n, const int32_t* path, int32_t len, int32_t* s_via, int* s_flags) {
+  int32_t* slot = t.store_path + (int64_t)n * t.slot_cap;
+  for (int i = threadIdx.x; i < len; i += blockDim.x) slot[i] = path[i];
+  __syncthreads();
+  const int rc = apply_path_dev(g, st, slot, len, t.net_id[n], +1, pa.pres_fac, pa.live,
+                                t.store_arcs + (int64_t)n * 2 * t.slot_cap, s_via, s_flags);
+  if (threadIdx.x == 0 && rc == OGR_OK) t.store_len[n] = len;
+  return rc;
+}
+
+// The ROI nets of a pass (pa.order[0..count)) in windows of mutually disjoint
+// footprints.  CTA 0 forms each window; CTA b rips up and searches its net
+// into scratch; then either every net commits (no failure) or CTA 0 commits in
+// order up to the first failed net, undoes the later nets' rip-ups and runs
+// the failed net's fallback.
+__global__ void __launch_bounds__(kThreads, 1)
+window_pass_kernel(ogr_graph g, ogr_state st, ogr_net_table t, ogr_pass_args pa, ogr_roi_batch rb, char* slot_base,
+                   size_t slot_bytes, int32_t rmax, int32_t* scratch, char* ctl_base, Ws w) {
+  __shared__ Shared sh;
+  __shared__ int32_t s_via[kMaxViaNodes];
+  __shared__ int s_flags[2];
+  __shared__ int s_bar;
+  __shared__ int s_box[4];
+  __shared__ int s_win[4];
+  WinCtl* c;
+  WinSlots ws;
+  win_ctl_layout(gridDim.x, ctl_base, &c, &ws);
+  const int b = blockIdx.x, tid = threadIdx.x, G = gridDim.x;
+  if (w.result[0] < 0) return;  // uniform: an earlier step of this pass failed
+  Ws mine;
+  ws_slot_layout(g.num_nodes, rmax, slot_base + (size_t)b * slot_bytes, &mine);
+  int32_t* my_path = scratch + (int64_t)b * t.slot_cap;
+  unsigned long long* stats = reinterpret_cast<unsigned long long*>(pa.stats);
+  const int32_t plane = g.nx * g.ny;
+  unsigned long long target = 0;
+  while (true) {
+    // 1. window formation (CTA 0)
+    if (b == 0) {
+      if (tid == 0) { s_win[0] = c->cursor; s_win[1] = 0; }
+      __syncthreads();
+      int k = s_win[0], W = 0;
+      while (k < pa.count && W < G) {
+        const int32_t n = pa.order[k];
+        const int32_t R = rb.roi_len[n];
+        if (R <= 0) {
+          if (W == 0) {
+            if (tid == 0) { ws.k[0] = k; ws.solo[0] = 1; }
+            W = 1;
+          }
+          break;
+        }
+        if (tid == 0) {
+          for (int q = 0; q < 4; ++q) s_box[q] = rb.roi_box[4 * n + q];
+        }
+        __syncthreads();
+        const int32_t ol = t.store_len[n];
+        const int32_t* op = t.store_path + (int64_t)n * t.slot_cap;
+        for (int i = tid; i < ol; i += kThreads) {
+          const int32_t r = op[i] % plane;
+          const int x = r % g.nx, y = r / g.nx;
+          atomicMin(&s_box[0], x); atomicMax(&s_box[1], x);
+          atomicMin(&s_box[2], y); atomicMax(&s_box[3], y);
+        }
+        __syncthreads();
+        bool clash = false;
+        for (int m = 0; m < W && !clash; ++m) clash = boxes_meet(s_box, ws.box + 4 * m);
+        if (clash) break;
+        if (tid == 0) {
+          ws.k[W] = k;
+          ws.solo[W] = 0;
+          for (int q = 0; q < 4; ++q) ws.box[4 * W + q] = s_box[q];
+        }
+        __syncthreads();
+        ++W;
+        ++k;
+      }
+      if (tid == 0) c->wsize = W;
+    }
+    if (!win_barrier(c, target, &s_bar)) break;
+    const int W = *(volatile int32_t*)&c->wsize;
+    if (W == 0 || *(volatile int32_t*)&c->error) break;
+    // 2. rip-up and search, one net per CTA, paths into scratch
+    if (b < W) {
+      const int32_t k = ws.k[b];
+      const int32_t n = pa.order[k];
+      const int32_t ol = t.store_len[n];
+      int rc = OGR_OK;
+      if (ol >= 2)
+        rc = apply_path_dev(g, st, t.store_path + (int64_t)n * t.slot_cap, ol, t.net_id[n], -1, pa.pres_fac,
+                            pa.live, nullptr, s_via, s_flags);
+      if (tid < 4) ws.stats[4 * b + tid] = 0ull;
+      __syncthreads();
+      if (rc == OGR_OK) {
+        const ogr_net_args a = ogr_pass_net_args(t, pa, n, 0);
+        if (ws.solo[b]) {
+          search_net(sh, g, st, a, w, my_path, t.slot_cap, ws.stats + 4 * b);
+        } else {
+          StageClock clk;
+          clk.start();
+          if (tid == 0) sh.status = OGR_OK;
+          __syncthreads();
+          sssp_roi(sh, g, st, a, mine, rb.roi_pool + (int64_t)n * rb.roi_cap, rb.roi_len[n], my_path, t.slot_cap,
+                   ws.stats + 4 * b, clk);
+        }
+        if (tid == 0) {
+          ws.st[b] = sh.status;
+          ws.len[b] = sh.len;
+          if (sh.status < 0) atomicExch(&c->error, sh.status);
+        }
+      } else if (tid == 0) {
+        atomicExch(&c->error, rc);
+      }
+    }
+    if (!win_barrier(c, target, &s_bar)) break;
+    if (*(volatile int32_t*)&c->error) break;
+    // 3. commit
+    int ff = W;
+    for (int m = 0; m < W; ++m)
+      if (ws.st[m] != OGR_OK) { ff = m; break; }
+    if (ff == W) {
+      if (b < W) {
+        const int32_t k = ws.k[b], n = pa.order[k];
+        const int rc = commit_from(g, st, t, pa, n, my_path, ws.len[b], s_via, s_flags);
+        if (tid < 4) atomicAdd(&stats[tid], ws.stats[4 * b + tid]);
+        if (tid == 0) {
+          pa.net_status[k] = 0;
+          if (rc != OGR_OK) atomicExch(&c->error, rc);
+          if (b == W - 1) c->cursor = k + 1;
+        }
+      }
+    } else if (b == 0) {
+      int rc = OGR_OK;
+      for (int m = 0; m < ff && rc == OGR_OK; ++m) {
+        const int32_t k = ws.k[m], n = pa.order[k];
+        rc = commit_from(g, st, t, pa, n, scratch + (int64_t)m * t.slot_cap, ws.len[m], s_via, s_flags);
+        if (tid < 4) atomicAdd(&stats[tid], ws.stats[4 * m + tid]);
+        if (tid == 0) pa.net_status[k] = 0;
+        __syncthreads();
+      }
+      for (int m = ff + 1; m < W && rc == OGR_OK; ++m) {   // undo the later rip-ups
+        const int32_t n = pa.order[ws.k[m]];
+        const int32_t ol = t.store_len[n];
+        if (ol >= 2)
+          rc = apply_path_dev(g, st, t.store_path + (int64_t)n * t.slot_cap, ol, t.net_id[n], +1, pa.pres_fac,
+                              pa.live, nullptr, s_via, s_flags);
+      }
+      const int32_t kf = ws.k[ff], nf = pa.order[kf];
+      if (tid < 4) atomicAdd(&stats[tid], ws.stats[4 * ff + tid]);
+      if (tid == 0) t.store_len[nf] = 0;
+      __syncthreads();
+      int flags = 0, fin = ws.st[ff], len = 0;
+      const int used = (int)w.result[2];
+      if (rc == OGR_OK && fin != OGR_OK && used < pa.fallback_quota) {
+        const ogr_net_args a = ogr_pass_net_args(t, pa, nf, 1);
+        search_net(sh, g, st, a, w, t.store_path + (int64_t)nf * t.slot_cap, t.slot_cap, stats);
+        fin = sh.status;
+        len = sh.len;
+        flags |= 2;
+        if (tid == 0) w.result[2] = used + 1;
+        if (fin < 0) rc = fin;
+      }
+      __syncthreads();
+      if (rc == OGR_OK && fin == OGR_OK) {
+        rc = apply_path_dev(g, st, t.store_path + (int64_t)nf * t.slot_cap, len, t.net_id[nf], +1, pa.pres_fac,
+                            pa.live, t.store_arcs + (int64_t)nf * 2 * t.slot_cap, s_via, s_flags);
+        if (tid == 0 && rc == OGR_OK) t.store_len[nf] = len;
+      } else {
+        flags |= 1;
+      }
+      if (tid == 0) {
+        pa.net_status[kf] = flags;
+        c->cursor = kf + 1;
+        if (rc != OGR_OK) atomicExch(&c->error, rc);
+      }
+    }
+    if (!win_barrier(c, target, &s_bar)) break;
+    if (*(volatile int32_t*)&c->error) break;
+  }
+  if (b == 0 && tid == 0) {
+    if (*(volatile int32_t*)&c->bar_err) w.result[0] = OGR_ERR_TIMEOUT;
+    else if (*(volatile int32_t*)&c->error) w.result[0] = *(volatile int32_t*)&c->error;
+  }
+}
+
+__global__ void window_ws_init_kernel(char* base, int32_t slots, size_t slot_bytes, int32_t N, int32_t rmax) {
+  for (int32_t sidx = 0; sidx < slots; ++sidx) {
+    Ws t;
+    ws_slot_layout(N, rmax, base + (size_t)sidx * slot_bytes, &t);
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x)
+      t.g2r[i] = -1;
+  }
+}
+
 // Long nets of a pass run as three launches each: this rip-up, the
 // whole-lattice search on every SM (fullgraph.cu), then pass_full_tail_kernel.
 __global__ void __launch_bounds__(kThreads, 1)
@@ -1051,6 +1355,23 @@ extern "C" int ogr_bfs_workspace_init(void* ws, int32_t num_nodes, int64_t qcap,
   OGR_LAUNCH_CHECK();
   return OGR_OK;
 }
+
+extern "C" size_t ogr_window_workspace_bytes(int32_t num_nodes, int32_t max_roi_nodes, int32_t slots) {
+  const int32_t r = max_roi_nodes < num_nodes ? max_roi_nodes : num_nodes;
+  return ws_slot_layout(num_nodes, r, nullptr, nullptr) * (size_t)(slots > 0 ? slots : 0);
+}
+
+extern "C" int ogr_window_workspace_init(void* ws, int32_t num_nodes, int32_t max_roi_nodes, int32_t slots,
+                                         void* stream) {
+  if (!ws || slots < 1 || num_nodes < 1 || max_roi_nodes < 1) return OGR_ERR_ARG;
+  const int32_t r = max_roi_nodes < num_nodes ? max_roi_nodes : num_nodes;
+  window_ws_init_kernel<<<ogr_blocks(num_nodes, 256), 256, 0, ogr_stream(stream)>>>(
+      (char*)ws, slots, ws_slot_layout(num_nodes, r, nullptr, nullptr), num_nodes, r);
+  OGR_LAUNCH_CHECK();
+  return OGR_OK;
+}
+
+extern "C" size_t ogr_window_ctl_bytes(int32_t slots) { return win_ctl_layout(slots, nullptr, nullptr, nullptr); }
 
 extern "C" int ogr_search_profile(int64_t* out16, int32_t reset) {
   if (!out16) return OGR_ERR_ARG;
@@ -1148,10 +1469,26 @@ extern "C" int ogr_path_apply(const ogr_graph* g, const ogr_state* st, const int
   return OGR_OK;
 }
 
+// Window-pass grid size: one 1024-thread CTA per SM, at most `slots`.
+static int window_grid(int slots) {
+  static int per_dev[64] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 0;
+  if (per_dev[dev] == 0) {
+    int sms = 0, per_sm = 0, coop = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
+    if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) != cudaSuccess || !coop) return 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, window_pass_kernel, kThreads, 0) != cudaSuccess)
+      return 0;
+    per_dev[dev] = sms * per_sm;
+  }
+  return slots < per_dev[dev] ? slots : per_dev[dev];
+}
+
 extern "C" int ogr_route_pass(const ogr_graph* g, const ogr_state* st, const ogr_net_table* t,
                               const ogr_pass_args* pa, const ogr_roi_batch* rb, void* ws, size_t bytes,
-                              const uint8_t* order_full, void* full_ws, size_t full_bytes, int32_t* status_out,
-                              void* stream) {
+                              const uint8_t* order_full, void* full_ws, size_t full_bytes,
+                              const ogr_window_args* win, int32_t* status_out, void* stream) {
   if (!g || !st || !t || !pa || !ws || !status_out) return OGR_ERR_ARG;
   if (bytes < ogr_route_workspace_bytes(g->num_nodes)) return OGR_ERR_CAPACITY;
   if (pa->count < 0 || t->slot_cap < 2) return OGR_ERR_ARG;
@@ -1181,9 +1518,41 @@ extern "C" int ogr_route_pass(const ogr_graph* g, const ogr_state* st, const ogr
     roi_batch_kernel<<<rbv.slots, kThreads, 0, s>>>(*g, *t, *pa, rbv);
     OGR_LAUNCH_CHECK();
   }
+  const bool windows = win != nullptr && win->slots > 0 && batch && rbv.roi_box != nullptr;
+  int grid = 0;
+  if (windows) {
+    if (!win->ws || !win->scratch || !win->ctl ||
+        win->slot_bytes < ogr_window_workspace_bytes(g->num_nodes, pa->max_roi_nodes, 1))
+      return OGR_ERR_ARG;
+    grid = window_grid(win->slots);
+    if (grid < 1) return OGR_ERR_CUDA;
+  }
+  // one run of ROI nets: batched windows, or the single-CTA sequential pass
+  auto roi_segment = [&](const ogr_pass_args& seg) -> int {
+    if (!windows) {
+      route_pass_kernel<<<1, kThreads, 0, s>>>(*g, *st, *t, seg, rbv, batch ? 1 : 0, w);
+      OGR_LAUNCH_CHECK();
+      return OGR_OK;
+    }
+    OGR_CUDA_TRY(cudaMemsetAsync(win->ctl, 0, ogr_window_ctl_bytes(grid), s));
+    ogr_graph gv = *g;
+    ogr_state sv = *st;
+    ogr_net_table tv = *t;
+    ogr_pass_args pv = seg;
+    char* slot_base = (char*)win->ws;
+    size_t slot_bytes = win->slot_bytes;
+    int32_t rmax = pa->max_roi_nodes < g->num_nodes ? pa->max_roi_nodes : g->num_nodes;
+    int32_t* scratch = win->scratch;
+    char* ctl = (char*)win->ctl;
+    Ws wv = w;
+    void* args[] = {&gv, &sv, &tv, &pv, &rbv, &slot_base, &slot_bytes, &rmax, &scratch, &ctl, &wv};
+    OGR_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)window_pass_kernel, dim3(grid), dim3(kThreads), args, 0,
+                                             s));
+    return OGR_OK;
+  };
   if (!any_full) {
-    route_pass_kernel<<<1, kThreads, 0, s>>>(*g, *st, *t, *pa, rbv, batch ? 1 : 0, w);
-    OGR_LAUNCH_CHECK();
+    const int rc = roi_segment(*pa);
+    if (rc != OGR_OK) return rc;
   } else {
     // Runs of ROI nets go through one single-CTA launch each; every long net
     // gets the whole GPU for its search.  Same order, same state updates.
@@ -1212,8 +1581,8 @@ extern "C" int ogr_route_pass(const ogr_graph* g, const ogr_state* st, const ogr
         seg.order = pa->order + k;
         seg.count = k1 - k;
         seg.net_status = pa->net_status + k;
-        route_pass_kernel<<<1, kThreads, 0, s>>>(*g, *st, *t, seg, rbv, batch ? 1 : 0, w);
-        OGR_LAUNCH_CHECK();
+        const int rc = roi_segment(seg);
+        if (rc != OGR_OK) return rc;
         k = k1;
       }
     }

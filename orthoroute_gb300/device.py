@@ -306,7 +306,7 @@ class PathStore:
     plus the per-net ROI pool and BFS slots of the batched ROI extraction."""
 
     def __init__(self, graph: DeviceGraph, num_nets: int, slot_cap: int = 8192, max_roi_nodes: int = 50_000,
-                 bfs_slots: int = 64):
+                 bfs_slots: int = 64, window_slots: int = 0):
         dev = graph.device
         lib = graph.lib
         self.num_nets = num_nets
@@ -326,10 +326,27 @@ class PathStore:
         self.bfs_ws = torch.empty(per * self.bfs_slots, dtype=torch.uint8, device=dev)
         _lib.check(lib.ogr_bfs_workspace_init(_p(self.bfs_ws), N, self.qcap, self.bfs_slots, None),
                    "ogr_bfs_workspace_init")
+        self.roi_box = torch.zeros(4 * num_nets, dtype=torch.int32, device=dev)
+        # batched disjoint-ROI windows: one search slot, scratch path and CTA per window member
+        self.window_slots = int(max(0, window_slots))
+        if self.window_slots:
+            self.win_slot_bytes = int(lib.ogr_window_workspace_bytes(N, max_roi_nodes, 1))
+            self.win_ws = torch.empty(self.win_slot_bytes * self.window_slots, dtype=torch.uint8, device=dev)
+            _lib.check(lib.ogr_window_workspace_init(_p(self.win_ws), N, max_roi_nodes, self.window_slots, None),
+                       "ogr_window_workspace_init")
+            self.win_scratch = torch.empty((self.window_slots, slot_cap), dtype=torch.int32, device=dev)
+            self.win_ctl = torch.empty(int(lib.ogr_window_ctl_bytes(self.window_slots)), dtype=torch.uint8,
+                                       device=dev)
 
     def roi_batch(self) -> _lib.RoiBatch:
         return _lib.RoiBatch(self.bfs_slots, self.slot_bytes, self.qcap, _p(self.bfs_ws), _p(self.roi_pool),
-                             _p(self.roi_len), self.roi_cap, _p(self.next))
+                             _p(self.roi_len), self.roi_cap, _p(self.next), _p(self.roi_box))
+
+    def window_args(self) -> Optional[_lib.WindowArgs]:
+        if not self.window_slots:
+            return None
+        return _lib.WindowArgs(self.window_slots, self.win_slot_bytes, _p(self.win_ws), _p(self.win_scratch),
+                               _p(self.win_ctl))
 
     def set_path(self, idx: int, path):
         n = len(path)
@@ -342,7 +359,7 @@ class PathStore:
 
 def route_pass(ops: "Ops", store: PathStore, table: dict, order: np.ndarray, *, fallback_quota, max_roi_nodes,
                owner_weight, path_weight, history_weight, pres_fac, live, penalty=True, batch_roi=True,
-               order_full: Optional[np.ndarray] = None):
+               order_full: Optional[np.ndarray] = None, windows: bool = True):
     """One ``ogr_route_pass`` call; returns (per-net status flags, stats[4]).
 
     order_full (host, one flag per entry of order) sends the full-graph nets
@@ -372,10 +389,11 @@ def route_pass(ops: "Ops", store: PathStore, table: dict, order: np.ndarray, *, 
     if order_full is not None and np.any(order_full):
         full_flags = np.ascontiguousarray(order_full, dtype=np.uint8)
         full_ws, full_bytes = _p(ops.full_workspace()), ops.full_ws_bytes
+    win = store.window_args() if (batch_roi and windows) else None
     rc = ops.lib.ogr_route_pass(C.byref(g), C.byref(st), C.byref(t), C.byref(a),
                                 C.byref(rb) if rb is not None else None, _p(ops.ws[0]), ops.ws_bytes,
                                 full_flags.ctypes.data if full_flags is not None else None, full_ws, full_bytes,
-                                C.byref(rc_dev), ops._sp())
+                                C.byref(win) if win is not None else None, C.byref(rc_dev), ops._sp())
     ops._ev1.record(stream)
     _lib.check(rc, "ogr_route_pass")
     ops._ev1.synchronize()

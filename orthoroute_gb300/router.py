@@ -267,7 +267,8 @@ class PathFinderRouter:
     """GB300 PathFinder router with the reference's Python API."""
 
     def __init__(self, config: Optional[PathFinderConfig] = None, use_gpu: Optional[bool] = None,
-                 device: str = "cuda", mode: str = "persistent", full_engine: str = "grid"):
+                 device: str = "cuda", mode: str = "persistent", full_engine: str = "grid",
+                 window_slots: int = 32):
         require_cuda()
         if mode not in ("persistent", "plain"):
             raise ValueError("mode must be 'persistent' (one launch per routing pass) or 'plain' (one per net)")
@@ -277,6 +278,7 @@ class PathFinderRouter:
         self.device = device
         self.mode = mode
         self.full_engine = full_engine
+        self.window_slots = int(window_slots)   # > 0: batched disjoint-ROI windows in persistent mode
         self.store: Optional[PathStore] = None
         self.lattice: Optional[Lattice] = None
         self.net_paths: Dict[str, List[int]] = {}
@@ -881,8 +883,9 @@ class PathFinderRouter:
         lengths = self.store.length.cpu().numpy()
         idx = torch.as_tensor(order.astype(np.int64), device=self.g.device)
         L = int(lengths[order].max()) if len(order) else 0
-        rows = self.store.path[idx, :max(L, 1)].cpu().numpy() if len(order) else None
-        arow = self.store.arcs[idx, :max(2 * (L - 1), 1)].cpu().numpy() if len(order) else None
+        rows = torch.index_select(self.store.path[:, :max(L, 1)], 0, idx).cpu().numpy() if len(order) else None
+        arow = (torch.index_select(self.store.arcs[:, :max(2 * (L - 1), 1)], 0, idx).cpu().numpy()
+                if len(order) else None)
         self.ops.counters["d2h_bytes"] += 4 * lengths.size + (rows.nbytes + arow.nbytes if rows is not None else 0)
         for k, name in enumerate(ordered):
             old = self.net_paths.get(name)
@@ -1193,7 +1196,8 @@ class PathFinderRouter:
         self._task_index = {n: i for i, n in enumerate(self._task_names)}
         if self.mode == "persistent":
             if self.store is None or self.store.num_nets != len(tasks):
-                self.store = PathStore(self.g, len(tasks))
+                self.store = PathStore(self.g, len(tasks),
+                                       window_slots=self.window_slots if self.mode == "persistent" else 0)
             self.store.length.zero_()
         self._edge_src_host = self.g.edge_src.cpu().numpy()
         self._indices_host = self.g.indices.cpu().numpy()

@@ -30,21 +30,22 @@ def flat(paths):
     return np.asarray(out, dtype=np.int64)
 
 
-def gpu_router(nx, ny, nz, iters, mode="persistent", full_engine="grid"):
+def gpu_router(nx, ny, nz, iters, mode="persistent", full_engine="grid", window_slots=32):
     from orthoroute_gb300 import Lattice
     from orthoroute_gb300.router import PathFinderConfig, PathFinderRouter
-    R = PathFinderRouter(PathFinderConfig(max_iterations=iters), mode=mode, full_engine=full_engine)
+    R = PathFinderRouter(PathFinderConfig(max_iterations=iters), mode=mode, full_engine=full_engine,
+                         window_slots=window_slots)
     R.initialize_lattice(Lattice(nx, ny, nz), board_bounds(nx, ny))
     return R
 
 
-@pytest.mark.parametrize("mode", ["persistent", "plain"])
+@pytest.mark.parametrize("mode,windows", [("persistent", 32), ("persistent", 0), ("plain", 0)])
 @pytest.mark.parametrize("tag", ["r0", "r1"])
-def test_gpu_router_matches_reference_runs(tag, mode):
+def test_gpu_router_matches_reference_runs(tag, mode, windows):
     m = META[tag]
     z = np.load(os.path.join(G, "runs.npz"))
     reqs = [(f"N{int(r[0])}", int(r[1]), int(r[2])) for r in z[f"{tag}_reqs"]]
-    R = gpu_router(m["nx"], m["ny"], m["nz"], m["iters"], mode)
+    R = gpu_router(m["nx"], m["ny"], m["nz"], m["iters"], mode, window_slots=windows)
     R.trace = []
     res = R.route_multiple_nets(reqs)
     n_ref = sum(1 for k in z.files if k.startswith(f"{tag}_it"))
