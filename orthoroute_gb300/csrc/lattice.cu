@@ -20,10 +20,15 @@ struct LatticeConst {
   int pptr[kMaxLayers + 1];
 };
 
-__constant__ LatticeConst c_lat;
-__constant__ int c_pz[kMaxPartners];
-__constant__ float c_pcost[kMaxPartners];
-__constant__ int c_psite[kMaxPartners];
+// The lattice description travels as a kernel argument and its via-partner
+// tables live in the build workspace, so builds on different streams (jobs
+// of a server) do not share state.
+struct LatDev {
+  LatticeConst h;
+  const int* pz;
+  const float* pcost;
+  const int* psite;
+};
 
 __device__ __forceinline__ bool site_ok(int mode, int x, int y) {
   if (mode == 0) return true;
@@ -33,35 +38,35 @@ __device__ __forceinline__ bool site_ok(int mode, int x, int y) {
 
 // Number of arcs and (optionally) the row itself.
 template <bool kWrite>
-__device__ __forceinline__ int node_row(int64_t n, int32_t* idx, float* cost, unsigned char* lay,
+__device__ __forceinline__ int node_row(const LatDev& L, int64_t n, int32_t* idx, float* cost, unsigned char* lay,
                                         unsigned char* kind) {
-  const int nx = c_lat.nx, ny = c_lat.ny;
+  const int nx = L.h.nx, ny = L.h.ny;
   const int64_t plane = (int64_t)nx * ny;
   const int z = (int)(n / plane);
   const int64_t r = n - (int64_t)z * plane;
   const int y = (int)(r / nx);
   const int x = (int)(r - (int64_t)y * nx);
   int k = 0;
-  const int p0 = c_lat.pptr[z], p1 = c_lat.pptr[z + 1];
+  const int p0 = L.h.pptr[z], p1 = L.h.pptr[z + 1];
   for (int p = p0; p < p1; ++p) {
-    const int zz = c_pz[p];
+    const int zz = L.pz[p];
     if (zz >= z) break;
-    if (!site_ok(c_psite[p], x, y)) continue;
+    if (!site_ok(L.psite[p], x, y)) continue;
     if (kWrite) {
       idx[k] = (int32_t)((int64_t)zz * plane + r);
-      cost[k] = c_pcost[p];
+      cost[k] = L.pcost[p];
       lay[k] = (unsigned char)z;
       kind[k] = 1;
     }
     ++k;
   }
-  const int ax = c_lat.axis[z];
+  const int ax = L.h.axis[z];
   if (ax != 0) {
-    const bool ww = c_lat.wrong_way_cost > 0.f;
+    const bool ww = L.h.wrong_way_cost > 0.f;
     const bool h = (ax == 1) || ww;
     const bool v = (ax == 2) || ww;
-    const float ch = (ax == 1) ? c_lat.lateral_cost : c_lat.wrong_way_cost;
-    const float cv = (ax == 2) ? c_lat.lateral_cost : c_lat.wrong_way_cost;
+    const float ch = (ax == 1) ? L.h.lateral_cost : L.h.wrong_way_cost;
+    const float cv = (ax == 2) ? L.h.lateral_cost : L.h.wrong_way_cost;
     if (v && y > 0) {
       if (kWrite) { idx[k] = (int32_t)(n - nx); cost[k] = cv; lay[k] = (unsigned char)z; kind[k] = 0; }
       ++k;
@@ -80,12 +85,12 @@ __device__ __forceinline__ int node_row(int64_t n, int32_t* idx, float* cost, un
     }
   }
   for (int p = p0; p < p1; ++p) {
-    const int zz = c_pz[p];
+    const int zz = L.pz[p];
     if (zz <= z) continue;
-    if (!site_ok(c_psite[p], x, y)) continue;
+    if (!site_ok(L.psite[p], x, y)) continue;
     if (kWrite) {
       idx[k] = (int32_t)((int64_t)zz * plane + r);
-      cost[k] = c_pcost[p];
+      cost[k] = L.pcost[p];
       lay[k] = (unsigned char)z;
       kind[k] = 1;
     }
@@ -94,10 +99,10 @@ __device__ __forceinline__ int node_row(int64_t n, int32_t* idx, float* cost, un
   return k;
 }
 
-__global__ void degree_kernel(int64_t N, int32_t* deg) {
+__global__ void degree_kernel(LatDev L, int64_t N, int32_t* deg) {
   for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < N;
        n += (int64_t)gridDim.x * blockDim.x)
-    deg[n] = node_row<false>(n, nullptr, nullptr, nullptr, nullptr);
+    deg[n] = node_row<false>(L, n, nullptr, nullptr, nullptr, nullptr);
 }
 
 // Exclusive scan, 3 phases: per-tile sums, scan of tile sums (1 block), add.
@@ -155,12 +160,12 @@ __global__ void scan_add(int32_t* out, int64_t N, const int32_t* tile_sums, cons
   }
 }
 
-__global__ void fill_kernel(int64_t N, const int32_t* indptr, int32_t* indices, float* cost,
+__global__ void fill_kernel(LatDev L, int64_t N, const int32_t* indptr, int32_t* indices, float* cost,
                             unsigned char* lay, unsigned char* kind, int32_t* edge_src) {
   for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < N;
        n += (int64_t)gridDim.x * blockDim.x) {
     const int64_t b = indptr[n];
-    const int k = node_row<true>(n, indices + b, cost + b, lay + b, kind + b);
+    const int k = node_row<true>(L, n, indices + b, cost + b, lay + b, kind + b);
     for (int j = 0; j < k; ++j) edge_src[b + j] = (int32_t)n;
   }
 }
@@ -178,9 +183,12 @@ __global__ void rev_kernel(int64_t N, const int32_t* indptr, const int32_t* indi
   }
 }
 
-int load_desc(const ogr_lattice_desc* d) {
+// Fills the description; the partner tables are copied on `s` into dev_tab
+// (3 * kMaxPartners words of the workspace).
+int load_desc(const ogr_lattice_desc* d, int* dev_tab, cudaStream_t s, LatDev* out) {
   if (!d || d->nx < 1 || d->ny < 1 || d->nz < 1 || d->nz > kMaxLayers) return OGR_ERR_ARG;
-  LatticeConst h{};
+  LatDev L{};
+  LatticeConst& h = L.h;
   h.nx = d->nx; h.ny = d->ny; h.nz = d->nz;
   h.lateral_cost = d->lateral_cost;
   h.wrong_way_cost = d->wrong_way_cost;
@@ -188,12 +196,17 @@ int load_desc(const ogr_lattice_desc* d) {
   for (int z = 0; z <= d->nz; ++z) h.pptr[z] = d->partner_ptr[z];
   const int np = d->partner_ptr[d->nz];
   if (np > kMaxPartners || np < 0) return OGR_ERR_ARG;
-  OGR_CUDA_TRY(cudaMemcpyToSymbol(c_lat, &h, sizeof(h)));
+  L.pz = dev_tab;
+  L.pcost = reinterpret_cast<const float*>(dev_tab + kMaxPartners);
+  L.psite = dev_tab + 2 * kMaxPartners;
   if (np > 0) {
-    OGR_CUDA_TRY(cudaMemcpyToSymbol(c_pz, d->partner_z, np * sizeof(int)));
-    OGR_CUDA_TRY(cudaMemcpyToSymbol(c_pcost, d->partner_cost, np * sizeof(float)));
-    OGR_CUDA_TRY(cudaMemcpyToSymbol(c_psite, d->partner_site, np * sizeof(int)));
+    OGR_CUDA_TRY(cudaMemcpyAsync(dev_tab, d->partner_z, np * sizeof(int), cudaMemcpyHostToDevice, s));
+    OGR_CUDA_TRY(cudaMemcpyAsync(dev_tab + kMaxPartners, d->partner_cost, np * sizeof(float),
+                                 cudaMemcpyHostToDevice, s));
+    OGR_CUDA_TRY(cudaMemcpyAsync(dev_tab + 2 * kMaxPartners, d->partner_site, np * sizeof(int),
+                                 cudaMemcpyHostToDevice, s));
   }
+  *out = L;
   return OGR_OK;
 }
 
@@ -234,15 +247,14 @@ extern "C" int ogr_csr_num_edges(const ogr_lattice_desc* d, int64_t* num_edges) 
 extern "C" size_t ogr_csr_workspace_bytes(const ogr_lattice_desc* d) {
   const int64_t N = (int64_t)d->nx * d->ny * d->nz;
   const int64_t tiles = (N + kScanTile - 1) / kScanTile;
-  return (size_t)(N * 4 + tiles * 4 + 64);
+  return (size_t)(N * 4 + tiles * 4 + 64) + 3 * sizeof(int) * kMaxPartners + 256;
 }
 
 extern "C" int ogr_csr_build(const ogr_lattice_desc* d, int32_t* indptr, int32_t* indices,
                              float* base_costs, uint8_t* edge_layer, uint8_t* edge_kind,
                              int32_t* edge_src, int32_t* rev, void* workspace,
                              size_t workspace_bytes, void* stream) {
-  int rc = load_desc(d);
-  if (rc != OGR_OK) return rc;
+  if (!d || d->nz > kMaxLayers || d->nz < 1) return OGR_ERR_ARG;
   const int64_t N = (int64_t)d->nx * d->ny * d->nz;
   if (N >= (int64_t)1 << 31) return OGR_ERR_ARG;
   const int64_t E = host_num_edges(d);
@@ -253,11 +265,15 @@ extern "C" int ogr_csr_build(const ogr_lattice_desc* d, int32_t* indptr, int32_t
   const int64_t tiles = (N + kScanTile - 1) / kScanTile;
   int32_t* tile_sums = deg + N;
   int32_t* total = tile_sums + tiles;
-  degree_kernel<<<ogr_blocks(N, 256), 256, 0, s>>>(N, deg);
+  const size_t tab_off = ((size_t)(N * 4 + tiles * 4 + 64) + 255) & ~(size_t)255;
+  LatDev L;
+  const int rc = load_desc(d, reinterpret_cast<int*>((char*)workspace + tab_off), s, &L);
+  if (rc != OGR_OK) return rc;
+  degree_kernel<<<ogr_blocks(N, 256), 256, 0, s>>>(L, N, deg);
   scan_tiles<<<(unsigned)tiles, kScanTile, 0, s>>>(deg, N, indptr, tile_sums);
   scan_tile_sums<<<1, kScanTile, 0, s>>>(tile_sums, tiles, total);
   scan_add<<<ogr_blocks(N + 1, 256), 256, 0, s>>>(indptr, N, tile_sums, total);
-  fill_kernel<<<ogr_blocks(N, 256), 256, 0, s>>>(N, indptr, indices, base_costs, edge_layer, edge_kind,
+  fill_kernel<<<ogr_blocks(N, 256), 256, 0, s>>>(L, N, indptr, indices, base_costs, edge_layer, edge_kind,
                                                   edge_src);
   if (rev) rev_kernel<<<ogr_blocks(N, 256), 256, 0, s>>>(N, indptr, indices, rev);
   OGR_LAUNCH_CHECK();

@@ -324,7 +324,7 @@ class PathStore:
         per = int(lib.ogr_bfs_workspace_bytes(N, self.qcap, 1))
         self.slot_bytes = per
         self.bfs_ws = torch.empty(per * self.bfs_slots, dtype=torch.uint8, device=dev)
-        _lib.check(lib.ogr_bfs_workspace_init(_p(self.bfs_ws), N, self.qcap, self.bfs_slots, None),
+        _lib.check(lib.ogr_bfs_workspace_init(_p(self.bfs_ws), N, self.qcap, self.bfs_slots, _stream_ptr(None)),
                    "ogr_bfs_workspace_init")
         self.roi_box = torch.zeros(4 * num_nets, dtype=torch.int32, device=dev)
         # batched disjoint-ROI windows: one search slot, scratch path and CTA per window member
@@ -332,7 +332,8 @@ class PathStore:
         if self.window_slots:
             self.win_slot_bytes = int(lib.ogr_window_workspace_bytes(N, max_roi_nodes, 1))
             self.win_ws = torch.empty(self.win_slot_bytes * self.window_slots, dtype=torch.uint8, device=dev)
-            _lib.check(lib.ogr_window_workspace_init(_p(self.win_ws), N, max_roi_nodes, self.window_slots, None),
+            _lib.check(lib.ogr_window_workspace_init(_p(self.win_ws), N, max_roi_nodes, self.window_slots,
+                                                     _stream_ptr(None)),
                        "ogr_window_workspace_init")
             self.win_scratch = torch.empty((self.window_slots, slot_cap), dtype=torch.int32, device=dev)
             self.win_ctl = torch.empty(int(lib.ogr_window_ctl_bytes(self.window_slots)), dtype=torch.uint8,

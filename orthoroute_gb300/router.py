@@ -519,7 +519,7 @@ class PathFinderRouter:
         cap = int(self._ov_idx.numel())
         _lib.check(lib.ogr_overused_arcs(self.E, self.s.present.data_ptr(), self.s.capacity.data_ptr(),
                                          self._ov_idx.data_ptr(), self._ov_val.data_ptr(), cap,
-                                         self._ov_cnt.data_ptr(), None), "ogr_overused_arcs")
+                                         self._ov_cnt.data_ptr(), self.ops._sp()), "ogr_overused_arcs")
         n = int(self._ov_cnt.item())
         if n > cap:
             raise RuntimeError("overused-arc buffer too small")
@@ -726,7 +726,8 @@ class PathFinderRouter:
             self._d_col_use.data_ptr(), self._d_col_cap.data_ptr(),
             self._d_seg_use.data_ptr() if seg else None, self._d_seg_cap.data_ptr() if seg else None,
             self._d_disc.data_ptr(), float(np.float32(1.0)), float(np.float32(1.0)), float(np.float32(pres_fac)),
-            int(bool(penalty)), int(bool(block)), self.s.total_cost.data_ptr(), None), "ogr_via_pools_apply")
+            int(bool(penalty)), int(bool(block)), self.s.total_cost.data_ptr(), self.ops._sp()),
+            "ogr_via_pools_apply")
         self.ops.sync_rcost()
 
     def _layer_bias_for_costs(self):
