@@ -43,6 +43,31 @@ CONFIGS = {
 }
 
 
+# serving stream: jobs arrive as a seeded Poisson process; each job's board is
+# one of three sizes with nets generated as in c0 (100x100x6) or c1 (larger)
+SERVE = dict(jobs=256, rate=4.0, seed=99, slots=4, budget_gb=160,
+             sizes=[dict(nx=100, ny=100, nz=6, nets=200, iters=10, clusters=False),
+                    dict(nx=300, ny=200, nz=8, nets=800, iters=40, clusters=True, via_span=4),
+                    dict(nx=600, ny=400, nz=12, nets=2000, iters=40, clusters=True, via_span=4)])
+
+
+def serve_jobs(n_jobs, iter_cap=None):
+    """The first n_jobs of the seeded serving stream (arrival times, boards, nets)."""
+    from orthoroute_gb300.serve import RouteJob, poisson_arrivals
+    arr = poisson_arrivals(SERVE["jobs"], SERVE["rate"], SERVE["seed"])
+    rng = np.random.default_rng(SERVE["seed"] + 1)
+    kinds = rng.integers(0, len(SERVE["sizes"]), size=SERVE["jobs"])
+    jobs = []
+    for i in range(n_jobs):
+        size = dict(SERVE["sizes"][int(kinds[i])])
+        size["seed"] = int(SERVE["seed"] * 1000 + i)
+        its = size["iters"] if iter_cap is None else min(size["iters"], iter_cap)
+        jobs.append(RouteJob(f"job{i}", size["nx"], size["ny"], size["nz"], make_requests(size),
+                             max_iterations=its, bounds=board_bounds(size["nx"], size["ny"]),
+                             allowed_via_spans=via_spans(size), arrival=float(arr[i])))
+    return jobs
+
+
 def via_spans(cfg):
     """allowed_via_spans of the lattice: the reference's default legal via
     pairs (layers 0..Nz-2, Lattice3D.get_legal_via_pairs) whose span |dz|
@@ -331,18 +356,61 @@ def run_reference(args, cfg):
             "e2e": {"value": round(v, 4), "unit": "s/job", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
+def run_serving(args):
+    """A bounded prefix of the serving stream through RouteServer: p50 / p99
+    job latency (arrival to completion) and jobs per second."""
+    import torch
+    from orthoroute_gb300.serve import RouteServer
+    warm = RouteServer(slots=1)
+    warm.run_stream(serve_jobs(1, iter_cap=2))      # loads the kernels once
+    warm.close()
+    torch.cuda.synchronize()
+    jobs = serve_jobs(args.serve_jobs, iter_cap=args.serve_iters)
+    srv = RouteServer(slots=SERVE["slots"], hbm_budget_bytes=SERVE["budget_gb"] << 30)
+    sampler = ClockSampler()
+    sampler.start()
+    t0 = time.perf_counter()
+    out = srv.run_stream(jobs)
+    wall = time.perf_counter() - t0
+    clocks = sampler.stop()
+    srv.close()
+    kinds = {}
+    for j in jobs:
+        kinds[f"{j.nx}x{j.ny}x{j.nz}"] = kinds.get(f"{j.nx}x{j.ny}x{j.nz}", 0) + 1
+    return {"metric": "serving stream: p99 job latency (arrival to completion)", "value": round(out["p99_s"], 4),
+            "unit": "s", "higher_is_better": False, "n_gpus": 1,
+            "p50_s": round(out["p50_s"], 4), "p99_s": round(out["p99_s"], 4),
+            "jobs_per_s": round(out["jobs_per_s"], 4), "errors": out["errors"],
+            "error_messages": sorted({r.error for r in out["results"] if r.error}),
+            "peak_concurrent_jobs": out["peak_concurrent"], "peak_hbm_gb": round(out["peak_hbm_bytes"] / 2 ** 30, 2),
+            "wall_s": round(wall, 3), "clocks": clocks, "data": "synthetic seeded job stream",
+            "config": {"workload": "c4", "jobs": len(jobs), "of_stream": SERVE["jobs"], "rate_per_s": SERVE["rate"],
+                       "iteration_cap": args.serve_iters, "slots": SERVE["slots"], "budget_gb": SERVE["budget_gb"],
+                       "boards": kinds,
+                       "sample": f"first {len(jobs)} jobs of the seeded {SERVE['jobs']}-job stream, "
+                                 f"negotiation capped at {args.serve_iters} iterations per job"}}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=None, help="timed jobs (default: 1 for c1, 3 for c0)")
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--config", default="c1", choices=sorted(CONFIGS))
+    ap.add_argument("--config", default="c1", choices=sorted(CONFIGS) + ["c4"])
+    ap.add_argument("--serve-jobs", type=int, default=16, help="c4: jobs of the stream to run")
+    ap.add_argument("--serve-iters", type=int, default=5, help="c4: iteration cap per job")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--mode", default="persistent", choices=["persistent", "plain"])
     ap.add_argument("--compare-plain", action="store_true", default=True)
     ap.add_argument("--no-compare-plain", dest="compare_plain", action="store_false")
     args = ap.parse_args()
+    if args.config == "c4":
+        if int(os.environ.get("RANK", "0")) == 0 and args.impl == "ours":
+            print(json.dumps(run_serving(args)), flush=True)
+        elif args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "the reference has no serving loop"}), flush=True)
+        return
     cfg = CONFIGS[args.config]
     if args.steps is None:
         args.steps = 1 if args.config == "c1" else 3

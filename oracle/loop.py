@@ -976,8 +976,9 @@ class OracleRouter:
             self.acc.update_costs(self.csr.base_costs, pres_fac, cfg.hist_cost_weight * 1.5,
                                   via_cost_multiplier=0.3, base_cost_weight=cfg.base_cost_weight)
             hot = self._build_hotset(ctasks, set())
-            if len(hot) > 60:
-                raise RuntimeError("detail-pass hotset above 60 nets depends on Python set order")
+            # unified_pathfinder.py:7672 keeps the first 60 nets of the set: the
+            # choice follows Python's string hashing (fix PYTHONHASHSEED to reproduce)
+            hot = set(list(hot)[:60])
             if not hot:
                 hot = cn
             sub = {k: v for k, v in ctasks.items() if k in hot}

@@ -1499,8 +1499,10 @@ class PathFinderRouter:
             self.ops.update_costs(pres_fac, cfg.hist_cost_weight * 1.5, 0.3, cfg.base_cost_weight, None)
             self._present_pres_fac = pres_fac
             hot = self._build_hotset(ctasks, set())
-            if len(hot) > 60:
-                raise RuntimeError("detail-pass hotset above 60 nets depends on Python set order")
+            # the reference keeps the first 60 nets of the set (:7672); which ones
+            # depends on Python's string hashing, here exactly as in the reference's
+            # process (set PYTHONHASHSEED for reproducible runs)
+            hot = set(list(hot)[:60])
             if not hot:
                 hot = cn
             sub = {k: v for k, v in ctasks.items() if k in hot}
