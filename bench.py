@@ -39,7 +39,9 @@ CONFIGS = {
     # plain_iters: the plain one-net-per-launch form is compared on the first iteration only
     # searches_per_job: searches of the (bit-identical) job, used to scale the CPU sample
     "c1": dict(nx=600, ny=400, nz=12, nets=2000, iters=40, seed=4321, clusters=True, via_span=4,
-               plain_iters=1, plain_nets=200, searches_per_job=10364),
+               plain_iters=1, plain_nets=200, searches_per_job=10364,
+               # DRAM bytes / algorithmic bytes of full_sssp_kernel, ncu on a 300x200x8 search
+               traffic_ratio=0.6655),
 }
 
 
@@ -290,7 +292,12 @@ def run_ours(args, cfg, rank, world):
         "sssp_gteps": round(gteps, 4),
         "searches_per_job": prof["searches"] // max(1, args.steps),
         "roofline": {"bound": "hbm", "achieved": round(achieved, 3), "peak": pk.get("hbm_gbs"), "unit": "GB/s",
-                     "frac": round(achieved / pk.get("hbm_gbs", 1.0), 6), "traffic": None,
+                     "frac": round(achieved / pk.get("hbm_gbs", 1.0), 6),
+                     "traffic": (round(cfg["traffic_ratio"] * alg_bytes / max(1, prof["searches"])) if
+                                 cfg.get("traffic_ratio") else None),
+                     "traffic_unit": "bytes per search (ncu DRAM bytes of full_sssp_kernel on a smaller "
+                                     "lattice, scaled by the algorithmic bytes)" if cfg.get("traffic_ratio")
+                                     else None,
                      "kernel": "search launches of the routing pass (full_sssp_kernel on all SMs for "
                                "full-graph nets, route_pass_kernel / roi_batch_kernel for ROI nets)",
                      "peak_kind": pk_kind,
