@@ -72,6 +72,12 @@ class Lattice:
         y, x = divmod(r, self.nx)
         return x, y, z
 
+    def allowed_axes(self, z: int) -> List[str]:
+        """Axes a planar move on layer z may take (``get_allowed_axes``)."""
+        axis = self.layer_dirs[z]
+        other = "v" if axis == "h" else "h"
+        return [axis] + ([other] if math.isfinite(self.wrong_way_cost_multiplier) else [])
+
     def lateral_layers(self) -> List[int]:
         return list(range(1, self.nz - 1)) if self.nz > 2 else list(range(self.nz))
 

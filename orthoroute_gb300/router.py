@@ -66,6 +66,8 @@ class PathFinderConfig:
         self.via_diameter = 0.25
         self.clearance = 0.15
         self.via_drill = 0.15
+        self.track_width = 0.24
+        self.layer_names: List[str] = ['F.Cu', 'In1.Cu', 'In2.Cu', 'In3.Cu', 'In4.Cu', 'B.Cu']
         self.min_hole_to_hole = 0.25
         self.stagnation_patience = 5
         self.slow_progress_window = 5
@@ -379,9 +381,16 @@ class PathFinderRouter:
         self.initialize_lattice(lat, bounds)
         return True
 
-    def initialize_lattice(self, lattice: Lattice, bounds=None):
+    def initialize_lattice(self, lattice: Lattice, bounds=None, layer_names: Optional[List[str]] = None):
         """Build the device CSR and congestion state for a lattice."""
         self.lattice = lattice
+        # copper layer names as initialize_graph derives them (:2883-2904)
+        names = list(layer_names) if layer_names else list(getattr(self.config, "layer_names", []) or [])
+        if len(names) != lattice.nz:
+            names = ["F.Cu"] + [f"In{i}.Cu" for i in range(1, lattice.nz - 1)] + (["B.Cu"] if lattice.nz > 1 else [])
+        self.config.layer_names = names
+        self._geometry_payload = GeometryPayload([], [])
+        self._provisional_geometry = GeometryPayload([], [])
         if bounds is None:
             p = lattice.pitch
             bounds = (0.0, 0.0, (lattice.nx - 1) * p, (lattice.ny - 1) * p)
@@ -1535,6 +1544,40 @@ class PathFinderRouter:
             pres_fac = min(pres_fac * 1.5, dmax)
         self._restore(best_state)
         return {'success': False, 'overuse_sum': best[1]}
+
+
+    # ------------------------------------------------------------- geometry (F4)
+    def emit_geometry(self, board=None) -> Tuple[int, int]:
+        """``emit_geometry`` (:11316-11404) for tuple requests: tracks and vias of
+        every routed path; the export payload is kept only without overuse."""
+        from .geometry import GridGeometry, generate_geometry
+        L = self.lattice
+        axes = [L.allowed_axes(z) for z in range(L.nz)]
+        tracks, vias = generate_geometry(self.net_paths, L.nx, L.ny, L.nz, axes, GridGeometry(self.bounds, L.pitch),
+                                         self.config.layer_names, self.config.track_width, self.config.via_diameter,
+                                         self.config.via_drill)
+        self._provisional_geometry = GeometryPayload(tracks, vias)
+        over_sum, _ = self._compute_overuse()
+        self._geometry_payload = GeometryPayload(tracks, vias) if over_sum == 0 else GeometryPayload([], [])
+        return len(tracks), len(vias)
+
+    def get_geometry_payload(self):
+        """Clean geometry when there is some, else the provisional one (:11638-11650)."""
+        if not self._geometry_payload.tracks and not self._geometry_payload.vias and \
+                (self._provisional_geometry.tracks or self._provisional_geometry.vias):
+            return self._provisional_geometry
+        return self._geometry_payload
+
+    def get_provisional_geometry(self):
+        return self._provisional_geometry
+
+
+class GeometryPayload:
+    """Tracks and vias with attribute access (the reference's class of this name, :548)."""
+
+    def __init__(self, tracks, vias):
+        self.tracks = tracks
+        self.vias = vias
 
 
 # the reference exports the same class under this name (:11661)

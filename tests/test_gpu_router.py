@@ -55,6 +55,13 @@ def test_gpu_router_matches_reference_runs(tag, mode, windows):
     for a, b in zip(res["iteration_metrics"], m["metrics"]):
         assert {k: a[k] for k in b} == b
     assert hashlib.sha256(flat(R.net_paths).tobytes()).hexdigest() == m["final_paths_sha"]
+    # F4: the emitted geometry equals the reference's on the same final paths
+    geo = json.load(open(os.path.join(G, "geometry.json")))[tag]
+    R.emit_geometry()
+    prov = R.get_provisional_geometry()
+    key = lambda d: json.dumps(d, sort_keys=True)
+    assert sorted(map(key, prov.tracks)) == sorted(map(key, geo["tracks"]))
+    assert sorted(map(key, prov.vias)) == sorted(map(key, geo["vias"]))
 
 
 def seeded_nets(nx, ny, n, seed, dmin=5, dmax=80):
