@@ -16,8 +16,10 @@ per-arc or per-node arrays runs on the device: cost update, via-pool
 penalties and hard block, live-present rebase, ROI BFS + exact SSSP +
 backtrace per net, commit / rip-up scatter, history, present EMA and the
 overuse / layer tallies.  Host mirrors hold only what the policy reads at
-path granularity (node ownership members, path-node use, node history, via
-pools).  There is no CPU routing fallback: a missing CUDA device raises.
+path granularity (path-node use, node history, via pools); barrel ownership,
+shared nodes and via-pool use are recomputed from one flat numpy view of all
+paths per change.  There is no CPU routing fallback: a missing CUDA device
+raises.
 """
 from __future__ import annotations
 
@@ -179,13 +181,126 @@ def _conflict_aware_hotset(ranked, pairs, cap, fraction, rng):
     return sel
 
 
-def _pair_combinations(members):
-    out = set()
-    s = sorted(members)
-    for i in range(len(s)):
-        for j in range(i + 1, len(s)):
-            out.add((s[i], s[j]))
-    return out
+def _sorted_unique(a):
+    """``np.unique`` of an integer array by one sort (NumPy 2's hashing
+    ``unique`` is many times slower on the path arrays here)."""
+    a = np.sort(np.asarray(a).ravel())
+    if a.size > 1:
+        a = a[np.concatenate(([True], a[1:] != a[:-1]))]
+    return a
+
+
+def _expand_ranges(lo, hi):
+    """Concatenation of arange(lo[i], hi[i]) over i."""
+    cnt = hi - lo
+    total = int(cnt.sum())
+    if total == 0:
+        return np.zeros(0, dtype=np.int64)
+    return np.repeat(lo - (np.cumsum(cnt) - cnt), cnt) + np.arange(total, dtype=np.int64)
+
+
+class _PathDict(dict):
+    """``net_paths`` (net name -> node list, the reference's dict) plus a
+    version that every assignment bumps and cached int64 node arrays per net,
+    from which the router's vectorised policy steps build one flat view of
+    all paths per version.  Paths are replaced, never edited in place."""
+
+    def __init__(self, *args, **kw):
+        super().__init__(*args, **kw)
+        self.version = 0
+        self._arrays: Dict[str, np.ndarray] = {}
+
+    def _touch(self, key):
+        self.version += 1
+        self._arrays.pop(key, None)
+
+    def __setitem__(self, key, value):
+        dict.__setitem__(self, key, value)
+        self._touch(key)
+
+    def set_path(self, key, value, array):
+        """Assign `value` together with its node array (int64, same nodes)."""
+        dict.__setitem__(self, key, value)
+        self._touch(key)
+        self._arrays[key] = array
+
+    def __delitem__(self, key):
+        dict.__delitem__(self, key)
+        self._touch(key)
+
+    def pop(self, key, *default):
+        out = dict.pop(self, key, *default)
+        self._touch(key)
+        return out
+
+    def popitem(self):
+        key, value = dict.popitem(self)
+        self._touch(key)
+        return key, value
+
+    def clear(self):
+        dict.clear(self)
+        self.version += 1
+        self._arrays.clear()
+
+    def update(self, *args, **kw):
+        for key, value in dict(*args, **kw).items():
+            self[key] = value
+
+    def setdefault(self, key, default=None):
+        if key not in self:
+            self[key] = default
+        return self[key]
+
+    def __ior__(self, other):
+        self.update(other)
+        return self
+
+    def array(self, key) -> np.ndarray:
+        a = self._arrays.get(key)
+        if a is None:
+            a = np.asarray(self.get(key) or (), dtype=np.int64)
+            self._arrays[key] = a
+        return a
+
+
+class _FlatPaths:
+    """Every path of two or more nodes of one ``net_paths`` version,
+    concatenated in dict order.  ``owner[i]`` is the position in ``names`` of
+    the net of node i, ``ids`` the nets' router ids, ``hops`` the positions i
+    where (i, i+1) is a via hop of one net (same (x, y), different z)."""
+
+    def __init__(self, paths: _PathDict, plane: int, net_id):
+        self.version = paths.version
+        self.plane = plane
+        self.names = [n for n, p in paths.items() if p is not None and len(p) >= 2]
+        arrs = [paths.array(n) for n in self.names]
+        k = len(arrs)
+        self.lens = np.fromiter((a.size for a in arrs), dtype=np.int64, count=k)
+        self.nodes = np.concatenate(arrs) if k else np.zeros(0, dtype=np.int64)
+        self.owner = np.repeat(np.arange(k, dtype=np.int64), self.lens)
+        self.ids = np.fromiter((net_id(n) for n in self.names), dtype=np.int64, count=k)
+        self.z, self.r = np.divmod(self.nodes, plane)
+        self.same = self.owner[:-1] == self.owner[1:]
+        self.hops = np.flatnonzero(self.same & (self.r[:-1] == self.r[1:]) & (self.z[:-1] != self.z[1:]))
+        self._via = None
+
+    def via_members(self):
+        """(node, net id) of every node spanned by a net's via hops (each
+        layer of the barrel), unique, sorted by node then id."""
+        if self._via is None:
+            h = self.hops
+            zu, zv = self.z[h], self.z[h + 1]
+            lo = np.minimum(zu, zv)
+            cnt = np.abs(zu - zv) + 1
+            rep = np.repeat(np.arange(h.size), cnt)
+            off = np.arange(int(cnt.sum()), dtype=np.int64) - np.repeat(np.cumsum(cnt) - cnt, cnt)
+            node = (lo[rep] + off) * self.plane + self.r[h][rep]
+            nid = self.ids[self.owner[h]][rep]
+            K = int(self.ids.max()) + 1 if self.ids.size else 1
+            key = _sorted_unique(node * K + nid)
+            self._via = (key // K, key % K)
+        return self._via
 
 
 class _ViaPools:
@@ -205,47 +320,40 @@ class _ViaPools:
             self.seg_prefix = np.zeros((nx, ny, self.segZ), dtype=np.float32)
             self.seg_pres_via = None
 
-    def rebuild(self, paths, plane, nx):
+    def rebuild(self, flat: _FlatPaths):
         """One column count per contiguous via run; its hull of segments
-        (``_accumulate_via_usage_for_path`` :4470-4546)."""
-        col = np.zeros((self.nx, self.ny), dtype=np.int16)
-        seg = np.zeros((self.nx, self.ny, self.segZ), dtype=np.int16) if self.has_seg else None
-        for p in paths:
-            if not p or len(p) < 2:
-                continue
-            a = np.asarray(p, dtype=np.int64)
-            z = a // plane
-            r = a % plane
-            via = (r[:-1] == r[1:]) & (z[:-1] != z[1:])
-            if not via.any():
-                continue
-            idx = np.flatnonzero(via)
-            # run starts: a via hop whose previous hop is not a via hop in the same column
-            start = np.ones(idx.size, dtype=bool)
-            start[1:] = ~((idx[1:] == idx[:-1] + 1) & (r[idx[1:]] == r[idx[:-1]]))
-            run_id = np.cumsum(start) - 1
-            xs = r[idx] % nx
-            ys = r[idx] // nx
-            zl = np.clip(np.minimum(z[idx], z[idx + 1]), 1, self.nz - 2)
-            zh = np.clip(np.maximum(z[idx], z[idx + 1]), 1, self.nz - 2)
-            for k in np.flatnonzero(start):
-                col[xs[k], ys[k]] += 1
-            if seg is not None:
-                nrun = int(run_id[-1]) + 1
-                lo = np.full(nrun, 1 << 30)
-                hi = np.full(nrun, -1)
-                np.minimum.at(lo, run_id, zl)
-                np.maximum.at(hi, run_id, zh)
-                rx = xs[start]
-                ry = ys[start]
-                for q in range(nrun):
-                    for zz in range(int(lo[q]), int(hi[q])):
-                        s = zz - 1
-                        if 0 <= s < self.segZ:
-                            seg[rx[q], ry[q], s] += 1
-        self.col_use[:] = col
-        if seg is not None:
-            self.seg_use[:] = seg
+        (``_accumulate_via_usage_for_path`` :4470-4546), over all paths at once."""
+        nx, ny = self.nx, self.ny
+        h = flat.hops
+        if h.size == 0:
+            self.col_use[:] = 0
+            if self.has_seg:
+                self.seg_use[:] = 0
+            return
+        r, z = flat.r, flat.z
+        # run starts: a via hop whose previous hop is not a via hop in the same
+        # column (adjacent hop positions always belong to one net)
+        start = np.ones(h.size, dtype=bool)
+        start[1:] = ~((h[1:] == h[:-1] + 1) & (r[h[1:]] == r[h[:-1]]))
+        rs = r[h[start]]
+        col = np.bincount(rs, minlength=nx * ny).reshape(ny, nx).T
+        self.col_use[:] = col.astype(np.int16)
+        if not self.has_seg:
+            return
+        zl = np.clip(np.minimum(z[h], z[h + 1]), 1, self.nz - 2)
+        zh = np.clip(np.maximum(z[h], z[h + 1]), 1, self.nz - 2)
+        first = np.flatnonzero(start)
+        lo = np.minimum.reduceat(zl, first)
+        hi = np.maximum.reduceat(zh, first)
+        cnt = np.maximum(hi - lo, 0)
+        rep = np.repeat(np.arange(first.size), cnt)
+        zz = lo[rep] + (np.arange(int(cnt.sum()), dtype=np.int64) - np.repeat(np.cumsum(cnt) - cnt, cnt))
+        s = zz - 1
+        ok = (s >= 0) & (s < self.segZ)
+        rr = rs[rep][ok]
+        flat_idx = ((rr % nx) * ny + rr // nx) * self.segZ + s[ok]
+        seg = np.bincount(flat_idx, minlength=nx * ny * self.segZ).reshape(nx, ny, self.segZ)
+        self.seg_use[:] = seg.astype(np.int16)
 
     def update_presence(self, alpha=0.6, beta=0.4):
         over = np.maximum(0, self.col_use - self.col_cap).astype(np.float32)
@@ -406,11 +514,12 @@ class PathFinderRouter:
         self.E = self.g.E
         self.pools = _ViaPools(L.nx, L.ny, L.nz)
         self.node_use = np.zeros(self.N, dtype=np.int16)
-        self.owner = np.full(self.N, -1, dtype=np.int32)
-        self.members: Dict[int, Set[int]] = {}
+        self._via_owner = np.full(self.N, -1, dtype=np.int64)
+        self._via_owner_set = np.zeros(0, dtype=np.int64)
         self.node_history = np.zeros(self.N, dtype=np.float32)
         self._hist_iter = None
-        self._hist_nodes: Set[int] = set()
+        self._hist_mask = np.zeros(self.N, dtype=bool)
+        self._flat_view = None
         self.layer_bias = np.ones(self.nz, dtype=np.float32)
         self._layer_bias_ema = None
         self.net_paths = {}
@@ -444,11 +553,9 @@ class PathFinderRouter:
         s.use_layer_bias = False
         self.pools = _ViaPools(self.nx, self.ny, self.nz)
         self.node_use.fill(0)
-        self.owner.fill(-1)
-        self.members = {}
         self.node_history.fill(0)
         self._hist_iter = None
-        self._hist_nodes = set()
+        self._hist_mask.fill(False)
         self.layer_bias = np.ones(self.nz, dtype=np.float32)
         self._layer_bias_ema = None
         self.net_paths = {}
@@ -520,7 +627,7 @@ class PathFinderRouter:
         rr = r[:-1][m]
         rep = np.repeat(np.arange(cnt.size), cnt)
         off = np.arange(int(cnt.sum())) - np.repeat(np.cumsum(cnt) - cnt, cnt)
-        return np.unique((lo[rep] + off) * self.plane + rr[rep]).tolist()
+        return _sorted_unique((lo[rep] + off) * self.plane + rr[rep]).tolist()
 
     def _overused(self):
         """(arc ids, over values) of every arc with present > capacity (device compaction)."""
@@ -542,44 +649,64 @@ class PathFinderRouter:
         return dict(zip(idx.tolist(), val.tolist())), idx, val
 
     # host mirrors of node state ------------------------------------------------
-    def _mark_nodes(self, name, path, sign):
-        nid = self._net_id(name)
-        nodes = np.unique(np.asarray(path, dtype=np.int64))
+    @property
+    def net_paths(self) -> Dict[str, List[int]]:
+        return self._net_paths
+
+    @net_paths.setter
+    def net_paths(self, value):
+        self._net_paths = value if isinstance(value, _PathDict) else _PathDict(value)
+
+    def _flat(self) -> _FlatPaths:
+        """The flat view of the current paths (rebuilt after any change)."""
+        f = self._flat_view
+        if f is None or f.version != self._net_paths.version or f.src is not self._net_paths:
+            f = _FlatPaths(self._net_paths, self.plane, self._net_id)
+            f.src = self._net_paths
+            self._flat_view = f
+        return f
+
+    def _mark_nodes(self, name, path, sign, array=None):
+        """path_node_use of one net's path (``_mark_path_node_use`` :4635);
+        the via-barrel ownership is derived from the paths when read."""
+        nodes = _sorted_unique(np.asarray(path, dtype=np.int64) if array is None else array)
         if sign > 0:
             self.node_use[nodes] += 1
         else:
             self.node_use[nodes] = np.maximum(self.node_use[nodes] - 1, 0)
-        for n in self._via_nodes(path):
-            if sign > 0:
-                m = self.members.setdefault(n, set())
-                m.add(nid)
-                self.owner[n] = nid if len(m) == 1 else -2
-            else:
-                m = self.members.get(n)
-                if not m:
-                    self.owner[n] = -1
-                    continue
-                m.discard(nid)
-                if not m:
-                    self.members.pop(n, None)
-                    self.owner[n] = -1
-                elif len(m) == 1:
-                    self.owner[n] = next(iter(m))
-                else:
-                    self.owner[n] = -2
+
+    def _via_owner_of(self, flat: _FlatPaths):
+        """Per-node barrel owner (``_mark_via_barrel_ownership_for_path``
+        :4934): -1 no via of any net, the net id for one net, -2 for several.
+        A dense node array of which only the nodes set last time are reset."""
+        vn, vid = flat.via_members()
+        own = self._via_owner
+        own[self._via_owner_set] = -1
+        if vn.size:
+            first = np.ones(vn.size, dtype=bool)
+            first[1:] = vn[1:] != vn[:-1]
+            starts = np.flatnonzero(first)
+            cnt = np.diff(np.append(starts, vn.size))
+            un = vn[starts]
+            own[un] = np.where(cnt == 1, vid[starts], -2)
+            self._via_owner_set = un
+        else:
+            self._via_owner_set = np.zeros(0, dtype=np.int64)
+        return own
 
     def _accumulate_history(self, nodes):
-        nodes = np.unique(np.asarray(list(nodes), dtype=np.int64))
+        """Node conflict history, once per node per iteration."""
+        nodes = _sorted_unique(np.asarray(nodes if isinstance(nodes, np.ndarray) else list(nodes), dtype=np.int64))
         if nodes.size == 0:
             return
         if self._hist_iter != self.iteration:
             self._hist_iter = self.iteration
-            self._hist_nodes = set()
-        nodes = np.asarray([n for n in nodes if int(n) not in self._hist_nodes], dtype=np.int64)
+            self._hist_mask.fill(False)
+        nodes = nodes[~self._hist_mask[nodes]]
         if nodes.size == 0:
             return
         self.node_history[nodes] += np.float32(self.config.node_history_increment)
-        self._hist_nodes.update(map(int, nodes))
+        self._hist_mask[nodes] = True
         d = torch.from_numpy(nodes).to(self.g.device)
         self.s.node_history[d] = torch.from_numpy(self.node_history[nodes]).to(self.g.device)
 
@@ -630,83 +757,100 @@ class PathFinderRouter:
         return over_sum + self.pools.spatial_overuse(), over_cnt
 
     def _path_node_overuse(self):
-        over = np.maximum(np.asarray(self.node_use, dtype=np.int64) - 1, 0)
-        return int(over.sum()), int(np.count_nonzero(over))
+        u = self.node_use[self.node_use > 1]
+        return int(u.sum(dtype=np.int64)) - u.size, int(u.size)
 
     def _path_node_conflicts(self):
+        """Shared path nodes (``_detect_path_node_conflicts`` :10564-10606):
+        (pairs of nets sharing a node, the shared nodes, shared-node count per net)."""
         shared = self.node_use > 1
         if not shared.any():
             return set(), set(), {}
-        members = defaultdict(set)
-        scores = defaultdict(int)
-        for name, path in self.net_paths.items():
-            if not path:
-                continue
-            nodes = np.unique(np.asarray(path, dtype=np.int32))
-            for n in nodes[shared[nodes]]:
-                members[int(n)].add(name)
-                scores[name] += 1
+        F = self._flat()
+        m = shared[F.nodes]
+        K = max(1, len(F.names))
+        key = _sorted_unique(F.nodes[m] * K + F.owner[m])
+        node, own = key // K, key % K
+        cnt = np.bincount(own, minlength=K)
+        scores = {F.names[i]: int(cnt[i]) for i in np.flatnonzero(cnt).tolist()}
         pairs = set()
-        for m in members.values():
-            pairs |= _pair_combinations(m)
-        return pairs, set(members), dict(scores)
+        if node.size:
+            first = np.ones(node.size, dtype=bool)
+            first[1:] = node[1:] != node[:-1]
+            starts = np.flatnonzero(first)
+            size = np.diff(np.append(starts, node.size))
+            pk = []
+            for k in _sorted_unique(size[size > 1]).tolist():
+                g = starts[size == k]
+                ii, jj = np.triu_indices(k, 1)
+                pk.append((own[g[:, None] + ii] * K + own[g[:, None] + jj]).ravel())
+            if pk:
+                names = F.names
+                for v in _sorted_unique(np.concatenate(pk)).tolist():
+                    x, y = names[v // K], names[v % K]
+                    pairs.add((x, y) if x <= y else (y, x))
+            shared_nodes = set(node[starts].tolist())
+        else:
+            shared_nodes = set()
+        return pairs, shared_nodes, scores
 
     def _detect_barrels(self):
         """Exact barrel conflicts + shared path nodes (``_detect_barrel_conflicts`` :10778-11111)."""
         self.barrel_conflict_nets, self.barrel_owner_nets, self.barrel_victim_nets = set(), set(), set()
         self.physical_scores = defaultdict(int)
         self.exact_pairs = set()
-        id_to_name = {v: k for k, v in self.net_id_map.items()}
-        srcs, dsts, nids = [], [], []
-        for name, path in self.net_paths.items():
-            if not path or len(path) < 2:
-                continue
-            a = np.asarray(path, dtype=np.int64)
-            srcs.append(a[:-1])
-            dsts.append(a[1:])
-            nids.append(np.full(len(path) - 1, self.net_id_map[name], dtype=np.int64))
+        F = self._flat()
         exact = 0
-        if srcs:
-            s = np.concatenate(srcs)
-            d = np.concatenate(dsts)
-            en = np.concatenate(nids)
-            so, do = self.owner[s], self.owner[d]
+        if F.names:
+            own = self._via_owner_of(F)
+            p = np.flatnonzero(F.same)          # hop (p, p+1) of one net
+            s, d = F.nodes[p], F.nodes[p + 1]
+            en = F.ids[F.owner[p]]
+            so, do = own[s], own[d]
             sc = (so != -1) & (so != en)
             dc = (do != -1) & (do != en)
             cm = sc | dc
             exact = int(cm.sum())
             if exact:
-                pos = np.flatnonzero(cm)
-                victims = set(map(int, en[pos]))
-                cnodes = np.unique(np.concatenate([s[sc], d[dc]]))
+                names_by_id = list(self.net_id_map)
+                victims = _sorted_unique(en[cm])
+                cnodes = _sorted_unique(np.concatenate([s[sc], d[dc]]))
                 self._accumulate_history(cnodes)
-                owners = set()
-                for n in cnodes:
-                    owners.update(self.members.get(int(n), ()))
-                for p in pos:
-                    vid = int(en[p])
-                    for n, flag in ((int(s[p]), sc[p]), (int(d[p]), dc[p])):
-                        if not flag:
-                            continue
-                        for oid in self.members.get(n, ()):
-                            if oid == vid:
-                                continue
-                            vn, on = id_to_name.get(vid), id_to_name.get(oid)
-                            if vn is not None and on is not None:
-                                self.physical_scores[vn] += 1
-                                self.physical_scores[on] += 1
-                                self.exact_pairs.add(tuple(sorted((vn, on))))
-                self.barrel_victim_nets = {id_to_name[i] for i in victims if i in id_to_name}
-                self.barrel_owner_nets = {id_to_name[i] for i in owners if i in id_to_name}
-                self.barrel_conflict_nets = {id_to_name[i] for i in (victims | owners) if i in id_to_name}
+                vn, vid = F.via_members()
+                lo = np.searchsorted(vn, cnodes, "left")
+                hi = np.searchsorted(vn, cnodes, "right")
+                owners = _sorted_unique(vid[_expand_ranges(lo, hi)])
+                # every (conflicting endpoint, other member of its barrel) counts
+                # once for both nets and names one exact pair
+                qn = np.concatenate([s[sc], d[dc]])
+                qv = np.concatenate([en[sc], en[dc]])
+                lo = np.searchsorted(vn, qn, "left")
+                hi = np.searchsorted(vn, qn, "right")
+                j = _expand_ranges(lo, hi)
+                victim = np.repeat(qv, hi - lo)
+                other = vid[j]
+                keep = other != victim
+                victim, other = victim[keep], other[keep]
+                K = len(names_by_id)
+                cnt = np.bincount(victim, minlength=K) + np.bincount(other, minlength=K)
+                for i in np.flatnonzero(cnt).tolist():
+                    self.physical_scores[names_by_id[i]] += int(cnt[i])
+                for v in _sorted_unique(np.minimum(victim, other) * K + np.maximum(victim, other)).tolist():
+                    x, y = names_by_id[v // K], names_by_id[v % K]
+                    self.exact_pairs.add((x, y) if x <= y else (y, x))
+                vset = {names_by_id[i] for i in victims.tolist()}
+                oset = {names_by_id[i] for i in owners.tolist()}
+                self.barrel_victim_nets = vset
+                self.barrel_owner_nets = oset
+                self.barrel_conflict_nets = vset | oset
         pairs, shared, pscores = self._path_node_conflicts()
         self.path_node_pairs = set(pairs)
         self.path_node_scores = dict(pscores)
         if shared:
             for name, sc_ in pscores.items():
                 self.physical_scores[name] += int(sc_)
-            self.barrel_conflict_nets.update({n for p in pairs for n in p})
-            self._accumulate_history(shared)
+            self.barrel_conflict_nets.update({n for p_ in pairs for n in p_})
+            self._accumulate_history(np.fromiter(shared, dtype=np.int64, count=len(shared)))
         return exact + len(shared)
 
     # ------------------------------------------------------------- device steps
@@ -897,17 +1041,18 @@ class PathFinderRouter:
         arow = (torch.index_select(self.store.arcs[:, :max(2 * (L - 1), 1)], 0, idx).cpu().numpy()
                 if len(order) else None)
         self.ops.counters["d2h_bytes"] += 4 * lengths.size + (rows.nbytes + arow.nbytes if rows is not None else 0)
+        paths = self._net_paths
         for k, name in enumerate(ordered):
-            old = self.net_paths.get(name)
+            old = paths.get(name)
             if old:
-                self._mark_nodes(name, old, -1)
+                self._mark_nodes(name, old, -1, paths.array(name))
                 self._clear_tracking(name)
             n = int(lengths[order[k]])
             if not (status[k] & 1) and n >= 2:
-                path = rows[k, :n].tolist()
+                arr = rows[k, :n].astype(np.int64)
                 edges = arow[k, :2 * (n - 1)].astype(np.int64)
-                self._mark_nodes(name, path, +1)
-                self.net_paths[name] = path
+                self._mark_nodes(name, None, +1, arr)
+                paths.set_path(name, arr.tolist(), arr)
                 self._update_tracking(name, edges)
             else:
                 self.net_paths[name] = []
@@ -968,21 +1113,15 @@ class PathFinderRouter:
         """Nets whose via hops use an over-full via column ("col", x, y) or a
         via segment ("seg", x, y, z-1) of z in [clamp(zlo), clamp(zhi))."""
         P = self.pools
-        names = [n for n, p in self.net_paths.items() if p and len(p) >= 2]
+        F = self._flat()
         members = defaultdict(set)
-        if not names:
+        h = F.hops
+        if h.size == 0:
             return members
-        arrs = [np.asarray(self.net_paths[n], dtype=np.int64) for n in names]
-        lens = np.fromiter((a.size for a in arrs), dtype=np.int64, count=len(arrs))
-        flat = np.concatenate(arrs)
-        owner = np.repeat(np.arange(len(names), dtype=np.int64), lens)
-        z, r = np.divmod(flat, self.plane)
-        hop = (owner[:-1] == owner[1:]) & (r[:-1] == r[1:]) & (z[:-1] != z[1:])
-        if not hop.any():
-            return members
-        ru = r[:-1][hop]
-        net = owner[:-1][hop]
-        zu, zv = z[:-1][hop], z[1:][hop]
+        names = F.names
+        ru = F.r[h]
+        net = F.owner[h]
+        zu, zv = F.z[h], F.z[h + 1]
         y, x = np.divmod(ru, self.nx)
         pairs = set()
         if col_over is not None:
@@ -1104,8 +1243,6 @@ class PathFinderRouter:
         self.s.owner_count.zero_()
         self.s.owner_xor.zero_()
         self.node_use.fill(0)
-        self.owner.fill(-1)
-        self.members = {}
         self.net_to_edges.clear()
         self._eidx = None
         if self.store is not None:
@@ -1118,7 +1255,7 @@ class PathFinderRouter:
         self._rebuild_via_usage()
 
     def _rebuild_via_usage(self):
-        self.pools.rebuild(list(self.net_paths.values()), self.plane, self.nx)
+        self.pools.rebuild(self._flat())
 
     def _rip_top_k(self, k=20):
         over_map, over_idx_arr, over_val_arr = self._over_map()

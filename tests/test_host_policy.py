@@ -1,12 +1,17 @@
 """Host-side policy helpers of the router (no GPU): the vectorised via-pool
-membership, barrel node expansion and per-net overuse sums agree with the
-per-hop loops they replace (the reference's own formulation)."""
+membership and usage, barrel node expansion, barrel ownership and conflicts,
+shared path nodes and per-net overuse sums agree with the per-hop loops they
+replace (the reference's own formulation, as the oracle restates it)."""
 from collections import defaultdict
+from types import SimpleNamespace
 
 import numpy as np
 import pytest
+import torch
 
 from orthoroute_gb300 import router as R
+from oracle.accounting import ViaPools as OracleViaPools
+from oracle.tallies import NodeState, detect_barrel_conflicts
 
 
 class _Host:
@@ -38,10 +43,156 @@ def _coord(h, n):
     return x, y, z
 
 
+def _router(nx=9, ny=7, nz=8):
+    """A router object with the host state only (no device)."""
+    h = object.__new__(R.PathFinderRouter)
+    h.nx, h.ny, h.nz, h.plane, h.N = nx, ny, nz, nx * ny, nx * ny * nz
+    h.config = R.PathFinderConfig()
+    h.pools = R._ViaPools(nx, ny, nz)
+    h.node_use = np.zeros(h.N, dtype=np.int16)
+    h._via_owner = np.full(h.N, -1, dtype=np.int64)
+    h._via_owner_set = np.zeros(0, dtype=np.int64)
+    h.node_history = np.zeros(h.N, dtype=np.float32)
+    h._hist_iter = None
+    h._hist_mask = np.zeros(h.N, dtype=bool)
+    h._flat_view = None
+    h.net_paths = {}
+    h.net_to_edges = {}
+    h._eidx = None
+    h.net_id_map = {}
+    h.iteration = 1
+    h.s = SimpleNamespace(node_history=torch.zeros(h.N, dtype=torch.float32))
+    h.g = SimpleNamespace(device="cpu")
+    h._reset_policy_state()
+    return h
+
+
+def _walk(rng, h, n, box):
+    """A simple path (no repeated node) of lateral steps and via hops in a small box."""
+    x, y = int(rng.integers(0, box)), int(rng.integers(0, box))
+    z = int(rng.integers(0, h.nz))
+    p, seen = [z * h.plane + y * h.nx + x], set()
+    seen.add(p[0])
+    for _ in range(n):
+        for _try in range(8):
+            if rng.random() < 0.35:
+                z2 = int(rng.integers(0, h.nz))
+                if z2 == z:
+                    continue
+                cand = (x, y, z2)
+            else:
+                dx, dy = [(1, 0), (-1, 0), (0, 1), (0, -1)][int(rng.integers(0, 4))]
+                cand = (min(max(x + dx, 0), box - 1), min(max(y + dy, 0), box - 1), z)
+            node = cand[2] * h.plane + cand[1] * h.nx + cand[0]
+            if node not in seen:
+                break
+        else:
+            break
+        x, y, z = cand
+        seen.add(node)
+        p.append(node)
+    return p
+
+
+def _routed(seed, nets=40, box=5):
+    rng = np.random.default_rng(seed)
+    h = _router()
+    paths = {}
+    for i in range(nets):
+        p = _walk(rng, h, int(rng.integers(0, 25)), box)
+        paths[f"N{(i * 7) % nets}"] = p if len(p) >= 2 and i % 9 else []    # the router stores no 1-node path
+    arcs_src, arcs_dst, edges = [], [], {}
+    for name, p in paths.items():
+        h._net_id(name)
+        if len(p) >= 2:
+            h._mark_nodes(name, p, +1)
+            ids = []
+            for u, v in list(zip(p, p[1:])) + list(zip(p[::-1], p[::-1][1:])):
+                ids.append(len(arcs_src))
+                arcs_src.append(u)
+                arcs_dst.append(v)
+            edges[name] = ids
+        h.net_paths[name] = p
+    return h, paths, np.asarray(arcs_src, dtype=np.int64), np.asarray(arcs_dst, dtype=np.int64), edges
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_barrel_conflicts_match_oracle_loops(seed):
+    h, paths, esrc, edst, edges = _routed(seed)
+    ns = NodeState(h.N, h.nx, h.plane)
+    ns.rebuild_owner([(h.net_id_map[n], p) for n, p in paths.items()])
+    ns.rebuild_use(paths.values())
+    np.testing.assert_array_equal(h.node_use, ns.path_node_use)
+    for rep in range(2):          # the second call sees this iteration's history marks
+        got = h._detect_barrels()
+        want, info = detect_barrel_conflicts(esrc, edst, ns, paths, edges, h.net_id_map, h.iteration)
+        assert got == want
+        assert info["exact"] > 0 and info["path_node"] > 0
+        assert h.barrel_victim_nets == info["victim_nets"]
+        assert h.barrel_owner_nets == info["owner_nets"]
+        assert h.barrel_conflict_nets == info["conflict_nets"]
+        assert h.exact_pairs == info["exact_pairs"]
+        assert h.path_node_pairs == info["path_node_pairs"]
+        assert h.path_node_scores == info["path_node_scores"]
+        assert dict(h.physical_scores) == dict(info["scores"])
+        np.testing.assert_array_equal(h.node_history, ns.node_history)
+        np.testing.assert_array_equal(h.s.node_history.numpy(), ns.node_history)
+        own = h._via_owner_of(h._flat())
+        np.testing.assert_array_equal(own, ns.owner)
+    # rip up some nets and reroute others: the flat view follows every change
+    for name in list(paths)[:10]:
+        if paths[name]:
+            h._mark_nodes(name, paths[name], -1)
+            ns.clear_use(paths[name])
+        h.net_paths[name] = []
+        paths[name] = []
+    h.iteration = 2
+    ns.rebuild_owner([(h.net_id_map[n], p) for n, p in paths.items()])
+    got = h._detect_barrels()
+    want, info = detect_barrel_conflicts(esrc, edst, ns, paths, edges, h.net_id_map, 2)
+    assert got == want and h.exact_pairs == info["exact_pairs"]
+    assert dict(h.physical_scores) == dict(info["scores"])
+    np.testing.assert_array_equal(h._via_owner_of(h._flat()), ns.owner)
+    np.testing.assert_array_equal(h.node_history, ns.node_history)
+
+
+@pytest.mark.parametrize("seed", range(4))
+def test_via_usage_rebuild_matches_oracle_loop(seed):
+    h, paths, *_ = _routed(seed, nets=60, box=6)
+    h._rebuild_via_usage()
+    ref = OracleViaPools(h.nx, h.ny, h.nz)
+    ref.rebuild(list(paths.values()))
+    assert ref.col_use.sum() > 0 and ref.seg_use.sum() > 0
+    np.testing.assert_array_equal(h.pools.col_use, ref.col_use)
+    np.testing.assert_array_equal(h.pools.seg_use, ref.seg_use)
+
+
+def test_path_dict_versions_and_arrays():
+    d = R._PathDict({"a": [1, 2]})
+    v = d.version
+    d["b"] = [3, 4, 5]
+    assert d.version > v and d.array("b").tolist() == [3, 4, 5]
+    d.set_path("b", [6, 7], np.asarray([6, 7], dtype=np.int64))
+    assert d.array("b").tolist() == [6, 7]
+    for op in (lambda: d.update({"c": [1, 2]}), lambda: d.pop("c"), lambda: d.setdefault("e", [8, 9]),
+               lambda: d.__delitem__("e"), d.clear):
+        v = d.version
+        op()
+        assert d.version > v
+    assert d.array("a").size == 0
+    h = _router()
+    h.net_paths = {"x": [0, h.plane, 2 * h.plane]}
+    assert isinstance(h.net_paths, R._PathDict)
+    f = h._flat()
+    assert f.names == ["x"] and f.hops.tolist() == [0, 1] and h._flat() is f
+    h.net_paths["y"] = [5, 6]
+    assert h._flat() is not f and h._flat().names == ["x", "y"]
+
+
 @pytest.mark.parametrize("seed", range(4))
 def test_via_pool_members_match_hop_loop(seed):
     rng = np.random.default_rng(seed)
-    h = _host()
+    h = _router()
     h.net_paths = {f"N{i}": _rand_path(rng, h, int(rng.integers(1, 30))) for i in range(40)}
     h.net_paths["N5"] = []
     col_over = rng.random((h.nx, h.ny)) < 0.3
