@@ -223,6 +223,28 @@ int ogr_find_path_roi(const ogr_graph* g, const float* costs, const int32_t* roi
                       size_t workspace_bytes, int32_t* path_out, int32_t path_cap,
                       int32_t* path_len_out, int64_t* stats, void* stream);
 
+/* The multi-source multi-sink seam, SimpleDijkstra.find_path_multisource_multisink(
+ * src_seeds, dst_targets, costs, roi_nodes, global_to_roi, node_penalty)
+ * (unified_pathfinder.py:2550-2659), used for portal-seeded nets (:8321,
+ * :8355): seeds (device int32[n_seeds], global ids) start with label
+ * seed_cost (device float64) + their node penalty; targets (device
+ * int32[n_targets]) are settled but never expanded, each with target_cost
+ * (device float64); the search exhausts the ROI and returns the path to the
+ * target with the least label + target cost (first in the heap's pop order
+ * among equals), seed first.  Seeds or targets outside the ROI are ignored;
+ * a repeated seed or target id is OGR_ERR_ARG.  The path's first and last
+ * nodes give the reference's entry and exit layers.  Workspace:
+ * ogr_multi_workspace_bytes (the route workspace + 16 bytes per node),
+ * initialised with ogr_route_workspace_init.  stats (may be NULL): arcs of
+ * the expanded nodes, nodes popped, ROI size, settle phases.  Synchronises. */
+size_t ogr_multi_workspace_bytes(int32_t num_nodes);
+int ogr_find_path_multi(const ogr_graph* g, const float* costs, const int32_t* roi_nodes, int32_t n_roi,
+                        const float* roi_penalty, const int32_t* seeds, const double* seed_cost,
+                        int32_t n_seeds, const int32_t* targets, const double* target_cost,
+                        int32_t n_targets, void* workspace, size_t workspace_bytes,
+                        int32_t* path_out, int32_t path_cap, int32_t* path_len_out,
+                        int64_t* stats, void* stream);
+
 /* Commit (sign=+1) or rip up (sign=-1) a path given as device node ids:
  * present +-1 (floored at 0), live-present refresh of those arcs when
  * live != 0, path-node use +-1, barrel ownership of every node spanned by a

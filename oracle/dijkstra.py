@@ -14,8 +14,8 @@ Semantics kept exactly:
 * backtrace walks ``parent`` from dst and reverses; a single-node path is
   ``None``.
 
-``find_path_roi_trace`` additionally returns the settled labels and the
-count of scanned arcs (the algorithmic edge count used for GTEPS).
+``find_path_multisource`` restates the multi-source multi-sink twin
+(``:2550-2659``) the same way.
 """
 from __future__ import annotations
 
@@ -78,6 +78,79 @@ def find_path_roi(indptr, indices, src, dst, costs, roi_nodes, global_to_roi,
         cur = int(parent[cur])
     path.reverse()
     return path if len(path) > 1 else None
+
+
+def find_path_multisource(indptr, indices, src_seeds, dst_targets, costs, roi_nodes, global_to_roi,
+                          node_penalty=None, plane=None, stats=None):
+    """``SimpleDijkstra.find_path_multisource_multisink``
+    (``unified_pathfinder.py:2550-2659``): seeds ``(global node, cost)``
+    start with label ``float(cost) + float(pen)`` (dist32 = float32 of it, no
+    parent); a target is popped but not expanded and keeps the first target
+    whose ``label + target cost`` is strictly below the best so far; the heap
+    runs until empty.  Returns ``(path, entry_layer, exit_layer)`` or None
+    (a one-node path is None)."""
+    R = len(roi_nodes)
+    dist = np.full(R, np.inf, dtype=np.float32)
+    parent = np.full(R, -1, dtype=np.int32)
+    visited = np.zeros(R, dtype=bool)
+    heap = []
+    for g, c in src_seeds:
+        r = int(global_to_roi[g])
+        if r >= 0:
+            sc = float(c)
+            if node_penalty is not None:
+                sc += float(node_penalty[r])
+            dist[r] = sc
+            heapq.heappush(heap, (sc, r))
+    targets = {}
+    for g, c in dst_targets:
+        r = int(global_to_roi[g])
+        if r >= 0:
+            targets[r] = (g, c)
+    if not heap or not targets:
+        return None
+    ip = indptr.tolist() if hasattr(indptr, "tolist") else indptr
+    best, best_total = None, np.inf
+    scanned = settled = 0
+    while heap:
+        du, u = heapq.heappop(heap)
+        if visited[u]:
+            continue
+        visited[u] = True
+        settled += 1
+        if u in targets:
+            total = du + targets[u][1]
+            if total < best_total:
+                best_total, best = total, u
+            continue
+        ug = int(roi_nodes[u])
+        for ei in range(ip[ug], ip[ug + 1]):
+            scanned += 1
+            v = int(global_to_roi[int(indices[ei])])
+            if v < 0 or visited[v]:
+                continue
+            alt = du + float(costs[ei])
+            if node_penalty is not None:
+                alt += float(node_penalty[v])
+            if alt < dist[v]:
+                dist[v] = alt
+                parent[v] = u
+                heapq.heappush(heap, (alt, v))
+    if stats is not None:
+        stats["scanned"] = stats.get("scanned", 0) + scanned
+        stats["settled"] = stats.get("settled", 0) + settled
+    if best is None:
+        return None
+    path, cur = [], best
+    while cur != -1:
+        path.append(int(roi_nodes[cur]))
+        cur = int(parent[cur])
+    path.reverse()
+    if len(path) <= 1:
+        return None
+    if plane:
+        return path, path[0] // plane, path[-1] // plane
+    return path, 0, 0
 
 
 # --- C restatement (same semantics, ~100x faster) ------------------------------

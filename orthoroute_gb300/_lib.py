@@ -13,6 +13,7 @@ from . import _build
 
 OGR_OK = 0
 OGR_NO_PATH = 1
+OGR_ERR_ARG = -1
 OGR_ERR_CAPACITY = -3
 OGR_NOALLOC_MAX_NODES = 262144
 ERRORS = {-1: "bad argument", -2: "CUDA error", -3: "buffer capacity exceeded",
@@ -28,6 +29,7 @@ EXPORTED = [
     "ogr_bfs_workspace_init", "ogr_full_workspace_bytes", "ogr_find_path_full",
     "ogr_full_profile", "ogr_full_workspace_init", "ogr_find_path_roi", "ogr_reverse_costs",
     "ogr_window_workspace_bytes", "ogr_window_workspace_init", "ogr_window_ctl_bytes",
+    "ogr_multi_workspace_bytes", "ogr_find_path_multi",
 ]
 
 P = C.c_void_p
@@ -134,6 +136,9 @@ def load(build_if_missing: bool = True):
         "ogr_window_ctl_bytes": [I32],
         "ogr_full_workspace_bytes": [I32, I64],
         "ogr_find_path_roi": [C.POINTER(Graph), P, P, I32, P, I32, I32, P, C.c_size_t, P, I32, C.POINTER(I32), P, P],
+        "ogr_multi_workspace_bytes": [I32],
+        "ogr_find_path_multi": [C.POINTER(Graph), P, P, I32, P, P, P, I32, P, P, I32, P, C.c_size_t, P, I32,
+                                C.POINTER(I32), P, P],
         "ogr_full_profile": [P, I32],
         "ogr_reverse_costs": [I64, P, P, P, P],
         "ogr_full_workspace_init": [P, C.c_size_t, I32, I64, P],

@@ -42,6 +42,12 @@ __device__ __forceinline__ float ogr_node_penalty(const ogr_state& st, const ogr
   return __fadd_rn(__fadd_rn(f, o), __fmul_rn(hist, a.history_weight));
 }
 
+// Any double to an unsigned key with the same order (negatives reversed).
+__device__ __forceinline__ unsigned long long ogr_order_bits(double d) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(d);
+  return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+
 // (a32, lu, u) lexicographic less-than.
 __device__ __forceinline__ bool ogr_key_lt(float a1, double l1, int32_t u1, float a2, double l2, int32_t u2) {
   if (a1 != a2) return a1 < a2;

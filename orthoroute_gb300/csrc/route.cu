@@ -44,7 +44,7 @@ constexpr int kThreads = 1024;
 constexpr int kWarps = kThreads / 32;
 constexpr int kSub = 16;                       // lanes per node
 constexpr int kGroups = kThreads / kSub;       // nodes in flight per CTA
-constexpr int32_t ST_NONE = 0, ST_FRONT = 1, ST_DONE = 2;
+constexpr int32_t ST_NONE = 0, ST_FRONT = 1, ST_DONE = 2, ST_SINK = 3;  // SINK: a settled target (multi-seed)
 constexpr int kMaxViaNodes = 4096;
 constexpr int kDMax = 32;                      // arcs per node the local adjacency holds
 constexpr int kAdjCap = 65536;                 // ROI nodes the local adjacency holds
@@ -74,6 +74,20 @@ struct Ws {
   int32_t* deg;      // [kAdjCap] arcs of the node
   int64_t* result;   // [0] status, [1] path len
   int64_t qcap;
+};
+
+// Seeds and targets of a multi-source multi-sink search
+// (find_path_multisource_multisink, unified_pathfinder.py:2550-2659), global
+// ids with FP64 costs, mapped to ROI-indexed arrays inside the search.
+struct MultiSeeds {
+  const int32_t* seeds;
+  const double* seed_cost;
+  int32_t nseeds;
+  const int32_t* targets;
+  const double* target_cost;
+  int32_t ntargets;
+  double* init;    // [R] seed cost before the node penalty, +inf for other nodes
+  double* tcost;   // [R] target cost, NaN for other nodes
 };
 
 __host__ __device__ constexpr size_t round256(size_t v) { return (v + 255) & ~(size_t)255; }
@@ -413,9 +427,18 @@ __device__ void roi_build(Shared& sh, const ogr_graph& g, const ogr_net_args& a,
 // ---- the search on a given ROI ---------------------------------------------------
 // roi[0..R) in ROI order (ignored when full).  Writes the path (global ids,
 // src first) to path_out and its length to sh.len, or a status to sh.status.
+//
+// With kMulti the search is the reference's multi-source multi-sink form: every
+// seed starts with label seed_cost + penalty and no parent (a first relaxation
+// that later ones must beat in float32), targets are settled but never
+// expanded, the search runs until nothing is left, and the result is the
+// settled target with the least (label + target cost), first in pop order
+// (label, ROI index) among equals.
+template <bool kMulti = false>
 __device__ void sssp_roi(Shared& sh, const ogr_graph& g, const ogr_state& st, const ogr_net_args& a, const Ws& w,
                          const int32_t* roi, int32_t R, int32_t* path_out, int32_t path_cap,
-                         unsigned long long* stats_acc, StageClock& clk, const float* roi_pen = nullptr) {
+                         unsigned long long* stats_acc, StageClock& clk, const float* roi_pen = nullptr,
+                         const MultiSeeds* ms = nullptr) {
   const int tid = threadIdx.x;
   const int lane = tid & 31, warp = tid >> 5;
   const int sl = tid & (kSub - 1), grp = tid / kSub;
@@ -438,6 +461,37 @@ __device__ void sssp_roi(Shared& sh, const ogr_graph& g, const ogr_state& st, co
   for (int r = tid; r < R; r += kThreads) {
     node[r].st = ST_NONE;
     node[r].stamp = -1;
+    if constexpr (kMulti) {
+      node[r].par = -1;
+      ms->init[r] = __longlong_as_double(0x7ff0000000000000ll);
+      ms->tcost[r] = __longlong_as_double(0x7ff8000000000000ll);
+    }
+  }
+  __syncthreads();
+  if constexpr (kMulti) {
+    // Seeds and targets outside the ROI are dropped (as the reference does);
+    // a repeated seed or target id is an argument error.
+    for (int i = tid; i < ms->nseeds; i += kThreads) {
+      const int32_t gid = ms->seeds[i];
+      if (gid < 0 || gid >= g.num_nodes) { sh.status = OGR_ERR_ARG; continue; }
+      const int32_t r = full ? gid : w.g2r[gid];
+      if (r < 0) continue;
+      if (atomicCAS(&node[r].stamp, -1, -2) != -1) { sh.status = OGR_ERR_ARG; continue; }
+      ms->init[r] = ms->seed_cost[i];
+    }
+    for (int i = tid; i < ms->ntargets; i += kThreads) {
+      const int32_t gid = ms->targets[i];
+      if (gid < 0 || gid >= g.num_nodes) { sh.status = OGR_ERR_ARG; continue; }
+      const int32_t r = full ? gid : w.g2r[gid];
+      if (r < 0) continue;
+      if (atomicCAS(&node[r].par, -1, -3) != -1) { sh.status = OGR_ERR_ARG; continue; }
+      ms->tcost[r] = ms->target_cost[i];
+    }
+    __syncthreads();
+    for (int r = tid; r < R; r += kThreads) {
+      node[r].stamp = -1;
+      node[r].par = -1;
+    }
   }
   __syncthreads();
   // ROI-local adjacency: neighbour ROI index and in-arc cost per slot.
@@ -463,15 +517,22 @@ __device__ void sssp_roi(Shared& sh, const ogr_graph& g, const ogr_state& st, co
     too_wide = __reduce_or_sync(0xffffffffu, too_wide);
     if (lane == 0 && too_wide) sh.local = 0;
   }
-  const int32_t rs = full ? src : w.g2r[src];
-  const int32_t rd = full ? dst : w.g2r[dst];
-  if (tid == 0 && (rs < 0 || rd < 0 || rs == rd)) sh.status = OGR_NO_PATH;
+  const int32_t rs = kMulti ? -1 : (full ? src : w.g2r[src]);
+  int32_t rd = kMulti ? -1 : (full ? dst : w.g2r[dst]);
+  if (!kMulti && tid == 0 && (rs < 0 || rd < 0 || rs == rd)) sh.status = OGR_NO_PATH;
   __syncthreads();
   const bool local = sh.local != 0;
   clk.mark(2);
   int phase = 0;
   if (sh.status == OGR_OK) {
-    if (tid == 0) {
+    if constexpr (kMulti) {
+      // the first recompute pass takes every seed (ROI order) from its initial
+      // candidate; nothing is settled yet
+      if (tid == 0) sh.ndirty = 0;
+      __syncthreads();
+      for (int r = tid; r < R; r += kThreads)
+        if (ms->init[r] < __longlong_as_double(0x7ff0000000000000ll)) w.dl[atomicAdd(&sh.ndirty, 1)] = r;
+    } else if (tid == 0) {
       node[rs].st = ST_DONE;
       node[rs].lab = 0.0;
       node[rs].m32 = 0.0f;
@@ -489,6 +550,7 @@ __device__ void sssp_roi(Shared& sh, const ogr_graph& g, const ogr_state& st, co
     double ld_stop = 0.0;
     while (true) {
       // 1. queue the unsettled ROI neighbours of the newly settled nodes
+      if (!(kMulti && phase == 0)) {
       if (tid == 0) sh.ndirty = 0;
       __syncthreads();
       const int nb = sh.nb;
@@ -498,7 +560,7 @@ __device__ void sssp_roi(Shared& sh, const ogr_graph& g, const ogr_state& st, co
           const int dx = w.deg[x];
           for (int k = sl; k < dx; k += kSub) {
             const int32_t y = w.adj[(int64_t)x * kDMax + k];
-            if (y < 0 || node[y].st == ST_DONE) continue;
+            if (y < 0 || node[y].st >= ST_DONE) continue;
             if (atomicExch(&node[y].stamp, phase) != phase) w.dl[atomicAdd(&sh.ndirty, 1)] = y;
           }
         } else {
@@ -507,10 +569,11 @@ __device__ void sssp_roi(Shared& sh, const ogr_graph& g, const ogr_state& st, co
           for (int32_t e = indptr[xg] + sl; e < e1; e += kSub) {
             const int32_t yg = indices[e];
             const int32_t y = full ? yg : w.g2r[yg];
-            if (y < 0 || node[y].st == ST_DONE) continue;
+            if (y < 0 || node[y].st >= ST_DONE) continue;
             if (atomicExch(&node[y].stamp, phase) != phase) w.dl[atomicAdd(&sh.ndirty, 1)] = y;
           }
         }
+      }
       }
       __syncthreads();
       clk.mark(3);
@@ -535,6 +598,17 @@ __device__ void sssp_roi(Shared& sh, const ogr_graph& g, const ogr_state& st, co
         double bl = 0.0;
         int32_t bu = 0x7fffffff;
         float cin = kInf;
+        if constexpr (kMulti) {
+          // the seed's own start: relaxed before any pop, so it wins float32 ties
+          if (valid && sl == 0) {
+            const double s0 = ms->init[y];
+            if (s0 < __longlong_as_double(0x7ff0000000000000ll)) {
+              ba = __double2float_rn(s0 + pd);
+              bl = -__longlong_as_double(0x7ff0000000000000ll);
+              bu = -1;
+            }
+          }
+        }
         if (valid) {
           if (local) {
             const int dy = w.deg[y];
@@ -542,6 +616,7 @@ __device__ void sssp_roi(Shared& sh, const ogr_graph& g, const ogr_state& st, co
               const int32_t u = w.adj[(int64_t)y * kDMax + k];
               if (u < 0) continue;
               const float c = w.acost[(int64_t)y * kDMax + k];
+              if (kMulti && node[u].st == ST_SINK) continue;   // targets relax nothing
               if (node[u].st != ST_DONE) {
                 cin = fminf(cin, c);
                 continue;
@@ -559,6 +634,7 @@ __device__ void sssp_roi(Shared& sh, const ogr_graph& g, const ogr_state& st, co
               const int32_t u = full ? ug : w.g2r[ug];
               if (u < 0) continue;
               const float c = st.rcost ? st.rcost[e] : st.total_cost[g.rev[e]];
+              if (kMulti && node[u].st == ST_SINK) continue;   // targets relax nothing
               if (node[u].st != ST_DONE) {
                 cin = fminf(cin, c);
                 continue;
@@ -585,7 +661,7 @@ __device__ void sssp_roi(Shared& sh, const ogr_graph& g, const ogr_state& st, co
           ns.cin = cin;
           if (ba < kInf) {
             ns.m32 = ba;
-            ns.lab = (bl + (double)bc) + pd;
+            ns.lab = (kMulti && bu == -1) ? ms->init[y] + pd : (bl + (double)bc) + pd;
             ns.par = bu;
             if (fresh) {
               ns.st = ST_FRONT;
@@ -599,7 +675,7 @@ __device__ void sssp_roi(Shared& sh, const ogr_graph& g, const ogr_state& st, co
       if (tid == 0) atomicAdd(&g_stage[13], (unsigned long long)nd);
       const int nf = sh.nfront;
       if (nf == 0) {
-        if (tid == 0) {
+        if (tid == 0 && !kMulti) {
           if (dst_done)
             sh.found = 1;
           else
@@ -629,8 +705,12 @@ __device__ void sssp_roi(Shared& sh, const ogr_graph& g, const ogr_state& st, co
         bool settle = (ns.lab == T);
         if (!settle) settle = ns.m32 < __double2float_rn((T + (double)ns.cin) + (double)ns.pen);
         if (settle) {
-          ns.st = ST_DONE;
-          w.blist[atomicAdd(&sh.nb, 1)] = x;
+          if (kMulti && ms->tcost[x] == ms->tcost[x]) {
+            ns.st = ST_SINK;   // settled, never expanded
+          } else {
+            ns.st = ST_DONE;
+            w.blist[atomicAdd(&sh.nb, 1)] = x;
+          }
         } else {
           w.fr[cur ^ 1][atomicAdd(&sh.nnext, 1)] = x;
         }
@@ -640,7 +720,7 @@ __device__ void sssp_roi(Shared& sh, const ogr_graph& g, const ogr_state& st, co
       cur ^= 1;
       clk.mark(6);
       if (tid == 0) atomicAdd(&g_stage[10], 1ull);
-      const bool done = !dst_done && node[rd].st == ST_DONE;
+      const bool done = !kMulti && !dst_done && node[rd].st == ST_DONE;
       const bool capped = phase + 1 > max_phase;
       if (done) ld_stop = node[rd].lab;
       __syncthreads();
@@ -659,9 +739,69 @@ __device__ void sssp_roi(Shared& sh, const ogr_graph& g, const ogr_state& st, co
     }
   }
   __syncthreads();
+  if constexpr (kMulti) {
+    // The reference keeps the first popped target whose label + target cost is
+    // strictly below the best so far: the least (total, label, ROI index).
+    if (sh.status == OGR_OK) {
+      unsigned long long k1 = ~0ull;
+      for (int r = tid; r < R; r += kThreads) {
+        if (node[r].st != ST_SINK) continue;
+        const double tot = node[r].lab + ms->tcost[r];
+        if (!(tot < __longlong_as_double(0x7ff0000000000000ll))) continue;
+        k1 = min(k1, ogr_order_bits(tot));
+      }
+      k1 = block_min_u64(k1, sh.s_min);
+      unsigned long long k2 = ~0ull;
+      if (k1 != ~0ull)
+        for (int r = tid; r < R; r += kThreads)
+          if (node[r].st == ST_SINK && ogr_order_bits(node[r].lab + ms->tcost[r]) == k1)
+            k2 = min(k2, ogr_order_bits(node[r].lab));
+      k2 = block_min_u64(k2, sh.s_min);
+      unsigned long long k3 = ~0ull;
+      if (k1 != ~0ull)
+        for (int r = tid; r < R; r += kThreads)
+          if (node[r].st == ST_SINK && ogr_order_bits(node[r].lab + ms->tcost[r]) == k1 &&
+              ogr_order_bits(node[r].lab) == k2)
+            k3 = min(k3, (unsigned long long)r);
+      k3 = block_min_u64(k3, sh.s_min);
+      if (tid == 0) {
+        if (k1 == ~0ull) {
+          sh.status = OGR_NO_PATH;
+        } else {
+          sh.found = 1;
+          sh.nb = (int)k3;   // the chosen target
+        }
+      }
+    }
+    __syncthreads();
+    if (sh.found) rd = sh.nb;
+    // every settled node was popped once; expanded ones scanned their row
+    if (sh.status == OGR_OK && stats_acc != nullptr) {
+      unsigned arcs = 0, pops = 0;
+      for (int r = tid; r < R; r += kThreads) {
+        const int32_t sr = node[r].st;
+        if (sr < ST_DONE) continue;
+        ++pops;
+        if (sr == ST_DONE) {
+          const int32_t rg = full ? r : roi[r];
+          arcs += (unsigned)(indptr[rg + 1] - indptr[rg]);
+        }
+      }
+      arcs = __reduce_add_sync(0xffffffffu, arcs);
+      pops = __reduce_add_sync(0xffffffffu, pops);
+      if (lane == 0) {
+        atomicAdd(&stats_acc[0], (unsigned long long)arcs);
+        atomicAdd(&stats_acc[1], (unsigned long long)pops);
+      }
+      if (tid == 0) {
+        atomicAdd(&stats_acc[2], (unsigned long long)R);
+        atomicAdd(&stats_acc[3], (unsigned long long)(phase + 1));
+      }
+    }
+  }
   // Arcs the sequential search scans before popping dst: the rows of all
   // nodes popped before it, i.e. settled with (L, idx) < (L(dst), dst).
-  if (sh.found && stats_acc != nullptr) {
+  if (!kMulti && sh.found && stats_acc != nullptr) {
     const double ld = node[rd].lab;
     unsigned arcs = 0, pops = 0;
     for (int r = tid; r < R; r += kThreads) {
@@ -830,6 +970,27 @@ find_path_given_roi_kernel(ogr_graph g, ogr_state st, ogr_net_args a, Ws w, cons
   }
   __syncthreads();
   sssp_roi(sh, g, st, a, w, roi, R, path_out, path_cap, reinterpret_cast<unsigned long long*>(stats), clk, roi_pen);
+  if (threadIdx.x == 0) {
+    w.result[0] = sh.status;
+    w.result[1] = sh.len;
+  }
+}
+
+// The multi-source multi-sink seam on a given ROI.
+__global__ void __launch_bounds__(kThreads, 1)
+find_path_multi_kernel(ogr_graph g, ogr_state st, ogr_net_args a, Ws w, const int32_t* roi, int32_t R,
+                       const float* roi_pen, MultiSeeds ms, int32_t* path_out, int32_t path_cap, int64_t* stats) {
+  __shared__ Shared sh;
+  StageClock clk;
+  clk.start();
+  if (threadIdx.x == 0) {
+    sh.status = OGR_OK;
+    sh.len = 0;
+    sh.found = 0;
+  }
+  __syncthreads();
+  sssp_roi<true>(sh, g, st, a, w, roi, R, path_out, path_cap, reinterpret_cast<unsigned long long*>(stats), clk,
+                 roi_pen, &ms);
   if (threadIdx.x == 0) {
     w.result[0] = sh.status;
     w.result[1] = sh.len;
@@ -1433,6 +1594,52 @@ extern "C" int ogr_find_path_roi(const ogr_graph* g, const float* costs, const i
   cudaStream_t s = ogr_stream(stream);
   find_path_given_roi_kernel<<<1, kThreads, 0, s>>>(*g, st, a, w, roi_nodes, n_roi, roi_penalty, path_out, path_cap,
                                                     stats);
+  OGR_LAUNCH_CHECK();
+  int64_t res[2];
+  OGR_CUDA_TRY(cudaMemcpyAsync(res, w.result, sizeof(res), cudaMemcpyDeviceToHost, s));
+  OGR_CUDA_TRY(cudaStreamSynchronize(s));
+  *path_len_out = (res[0] == OGR_OK) ? (int32_t)res[1] : 0;
+  return (int)res[0];
+}
+
+extern "C" size_t ogr_multi_workspace_bytes(int32_t num_nodes) {
+  return ogr_route_workspace_bytes(num_nodes) + 2 * round256(8 * (size_t)(num_nodes > 0 ? num_nodes : 0));
+}
+
+extern "C" int ogr_find_path_multi(const ogr_graph* g, const float* costs, const int32_t* roi_nodes, int32_t n_roi,
+                                   const float* roi_penalty, const int32_t* seeds, const double* seed_cost,
+                                   int32_t n_seeds, const int32_t* targets, const double* target_cost,
+                                   int32_t n_targets, void* ws, size_t bytes, int32_t* path_out, int32_t path_cap,
+                                   int32_t* path_len_out, int64_t* stats, void* stream) {
+  if (!g || !costs || !roi_nodes || !ws || !path_out || !path_len_out || n_roi < 0 || n_roi > g->num_nodes ||
+      n_seeds < 0 || n_targets < 0 || (n_seeds > 0 && (!seeds || !seed_cost)) ||
+      (n_targets > 0 && (!targets || !target_cost)))
+    return OGR_ERR_ARG;
+  if (bytes < ogr_multi_workspace_bytes(g->num_nodes)) return OGR_ERR_CAPACITY;
+  *path_len_out = 0;
+  if (n_roi == 0 || n_seeds == 0 || n_targets == 0) return OGR_NO_PATH;
+  Ws w;
+  const size_t base = ws_layout(g->num_nodes, (char*)ws, &w);
+  MultiSeeds ms{};
+  ms.seeds = seeds;
+  ms.seed_cost = seed_cost;
+  ms.nseeds = n_seeds;
+  ms.targets = targets;
+  ms.target_cost = target_cost;
+  ms.ntargets = n_targets;
+  ms.init = (double*)((char*)ws + base);
+  ms.tcost = (double*)((char*)ws + base + round256(8 * (size_t)g->num_nodes));
+  ogr_state st{};
+  st.total_cost = const_cast<float*>(costs);
+  ogr_net_args a{};
+  a.net_id = -1;
+  a.src = -1;
+  a.dst = -1;
+  a.full_graph = 0;
+  a.penalty_enabled = 0;
+  cudaStream_t s = ogr_stream(stream);
+  find_path_multi_kernel<<<1, kThreads, 0, s>>>(*g, st, a, w, roi_nodes, n_roi, roi_penalty, ms, path_out, path_cap,
+                                                stats);
   OGR_LAUNCH_CHECK();
   int64_t res[2];
   OGR_CUDA_TRY(cudaMemcpyAsync(res, w.result, sizeof(res), cudaMemcpyDeviceToHost, s));

@@ -272,6 +272,48 @@ class Ops:
             return None
         return self.path_buf[: n.value].cpu().tolist()
 
+    def multi_workspace(self) -> torch.Tensor:
+        """Scratch of the multi-source search (allocated on first use)."""
+        if getattr(self, "_multi_ws", None) is None:
+            self.multi_ws_bytes = int(self.lib.ogr_multi_workspace_bytes(self.g.N))
+            self._multi_ws = torch.empty(self.multi_ws_bytes, dtype=torch.uint8, device=self.g.device)
+            _lib.check(self.lib.ogr_route_workspace_init(_p(self._multi_ws), self.multi_ws_bytes, self.g.N,
+                                                         self._sp()), "ogr_route_workspace_init")
+        return self._multi_ws
+
+    def find_path_multi(self, src_seeds, dst_targets, costs: torch.Tensor, roi_nodes, roi_penalty=None):
+        """``SimpleDijkstra.find_path_multisource_multisink`` seam: seeds and
+        targets are ``(global node, cost)`` pairs; a repeated target keeps its
+        last cost (the reference builds a dict).  Returns ``(path,
+        entry_layer, exit_layer)`` or None."""
+        dev = self.g.device
+        tg = dict((int(n), float(c)) for n, c in dst_targets)
+        seeds = [(int(n), float(c)) for n, c in src_seeds]
+        if len({n for n, _ in seeds}) != len(seeds):
+            raise ValueError("repeated seed node")
+        if not seeds or not tg:
+            return None
+        roi = torch.as_tensor(np.asarray(roi_nodes, dtype=np.int32)).to(dev)
+        pen = None if roi_penalty is None else torch.as_tensor(np.asarray(roi_penalty, dtype=np.float32)).to(dev)
+        sd = torch.as_tensor(np.asarray([n for n, _ in seeds], dtype=np.int32)).to(dev)
+        sc = torch.as_tensor(np.asarray([c for _, c in seeds], dtype=np.float64)).to(dev)
+        td = torch.as_tensor(np.asarray(list(tg), dtype=np.int32)).to(dev)
+        tc = torch.as_tensor(np.asarray(list(tg.values()), dtype=np.float64)).to(dev)
+        ws = self.multi_workspace()
+        g = self.g.cgraph()
+        n = C.c_int32(0)
+        rc = self.lib.ogr_find_path_multi(C.byref(g), _p(costs), _p(roi), int(roi.numel()), _p(pen), _p(sd), _p(sc),
+                                          int(sd.numel()), _p(td), _p(tc), int(td.numel()), _p(ws),
+                                          self.multi_ws_bytes, _p(self.path_buf), int(self.path_buf.numel()),
+                                          C.byref(n), _p(self.stats), self._sp())
+        _lib.check(rc, "ogr_find_path_multi")
+        self.counters["launches"] += 1
+        if rc == _lib.OGR_NO_PATH or n.value < 2:
+            return None
+        path = self.path_buf[: n.value].cpu().tolist()
+        plane = self.g.lattice.plane
+        return path, path[0] // plane, path[-1] // plane
+
     def extract_roi(self, net: _lib.NetArgs, slot: int = 0) -> np.ndarray:
         g = self.g.cgraph()
         out = torch.empty(self.g.N, dtype=torch.int32, device=self.g.device)

@@ -161,3 +161,30 @@ def test_c_heap_dijkstra_matches_reference(roi_lattice, i):
     p2 = find_path_roi_c(g.indptr, g.indices, s, d, costs, roi, g2r, node_penalty=pen, stats=st_c)
     np.testing.assert_array_equal(np.asarray(p2 or [], dtype=np.int32), z[f"s{i}_path"])
     assert p1 == p2 and st_py == st_c
+
+
+def multisource_case(g, z, i):
+    """Inputs of golden multi-source case i (arc costs regenerated from the seed)."""
+    from tests.golden.make_multisource_golden import multisource_costs
+    costs = multisource_costs(len(g.indices), i)
+    roi = z[f"m{i}_roi"]
+    g2r = np.full(g.num_nodes, -1, dtype=np.int32)
+    g2r[roi] = np.arange(len(roi), dtype=np.int32)
+    seeds = list(zip(z[f"m{i}_seeds"].tolist(), z[f"m{i}_seed_cost"].tolist()))
+    targets = list(zip(z[f"m{i}_targets"].tolist(), z[f"m{i}_target_cost"].tolist()))
+    pen = z[f"m{i}_pen"] if f"m{i}_pen" in z else None
+    return costs, roi, g2r, seeds, targets, pen
+
+
+@pytest.mark.parametrize("i", range(10))
+def test_multisource_matches_reference(roi_lattice, i):
+    """find_path_multisource_multisink of the reference on portal-like seed columns."""
+    from oracle.dijkstra import find_path_multisource
+    g = roi_lattice
+    z = np.load(os.path.join(G, "multisource.npz"))
+    costs, roi, g2r, seeds, targets, pen = multisource_case(g, z, i)
+    res = find_path_multisource(g.indptr, g.indices, seeds, targets, costs, roi, g2r, node_penalty=pen,
+                                plane=g.plane)
+    path, ent, exl = res if res else ([], -1, -1)
+    np.testing.assert_array_equal(np.asarray(path, dtype=np.int32), z[f"m{i}_path"])
+    assert [ent, exl] == z[f"m{i}_layers"].tolist()
