@@ -199,7 +199,8 @@ def run_ours(args, cfg, rank, world):
         router.initialize_state()
         return router.route_multiple_nets(reqs)
 
-    router = PathFinderRouter(PathFinderConfig(max_iterations=cfg["iters"]), mode=args.mode)
+    router = PathFinderRouter(PathFinderConfig(max_iterations=cfg["iters"]), mode=args.mode,
+                              full_engine=args.full_engine)
     router.initialize_lattice(make_lattice(cfg), bounds)
     for _ in range(args.warmup):
         job(router)
@@ -229,7 +230,8 @@ def run_ours(args, cfg, rank, world):
     for _ in range(max(1, min(args.steps, 2))):
         torch.cuda.synchronize()
         t1 = time.perf_counter()
-        r2 = PathFinderRouter(PathFinderConfig(max_iterations=cfg["iters"]), mode=args.mode)
+        r2 = PathFinderRouter(PathFinderConfig(max_iterations=cfg["iters"]), mode=args.mode,
+                              full_engine=args.full_engine)
         r2.initialize_lattice(make_lattice(cfg), bounds)
         res2 = r2.route_multiple_nets(reqs)
         _ = {k: list(v) for k, v in res2["paths"].items()}
@@ -308,6 +310,10 @@ def run_ours(args, cfg, rank, world):
         "gpu_launches": prof["launches"] // max(1, args.steps),
         "clocks": clocks,
         "mode": args.mode,
+        "full_engine": {"requested": args.full_engine, "used": router.full_engine,
+                        "tuning": (None if router.tuning is None else
+                                   {"ctas": router.tuning.full_ctas, "ms_per_search": router.tuning.ms_per_search,
+                                    "cached": router.tuning.cached})},
     }
     if plain is not None:
         if "batched_s" not in plain:
@@ -409,6 +415,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--mode", default="persistent", choices=["persistent", "plain"])
+    ap.add_argument("--full-engine", default="auto", choices=["auto", "grid", "cta"],
+                    help="engine of full-graph nets; auto = autotuned per lattice")
     ap.add_argument("--compare-plain", action="store_true", default=True)
     ap.add_argument("--no-compare-plain", dest="compare_plain", action="store_false")
     args = ap.parse_args()

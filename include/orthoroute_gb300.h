@@ -376,6 +376,14 @@ int ogr_find_path_full(const ogr_graph* g, const ogr_state* st, const ogr_net_ar
                        void* workspace, size_t workspace_bytes, int32_t* path_out,
                        int32_t path_cap, int32_t* path_len_out, int64_t* stats, void* stream);
 
+/* Grid of the whole-lattice search on the current device (a tuning knob;
+ * results do not depend on it): ctas > 0 sets the number of cooperative CTAs
+ * (at most *limit = SMs x resident CTAs per SM), 0 only reads.  *current and
+ * *limit (host, may be NULL) receive the grid in use and the maximum.  The
+ * setting is per device and process-wide.  Chosen by the autotuner
+ * (orthoroute_gb300/autotune.py); no reference counterpart. */
+int ogr_full_grid(int32_t ctas, int32_t* current, int32_t* limit);
+
 /* Tracing of the whole-lattice search (host int64[8], cumulative since the
  * last reset): searches, phases, kernel ns, init ns, E-step work ns and
  * S-step work ns of the busiest CTA, barrier wait ns and statistics +

@@ -1,0 +1,150 @@
+"""Autotuner for the whole-lattice search: engine and CTA grid per lattice size.
+
+Full-graph nets (Manhattan length >= 125, ``_route_all`` :8219-8262) are
+searched either by ``full_sssp_kernel`` on a cooperative grid of CTAs (one
+grid step per settle phase) or by a single 1024-thread CTA.  Which one is
+faster, and with how many CTAs, depends on the lattice: a grid step costs a
+grid-wide barrier (more CTAs, dearer barrier) and spreads the phase's front
+over the CTAs (more CTAs, less work each).  The exact search has no bucket
+width to tune: each phase's threshold is the least tentative label, and the
+settle rule is fixed by exactness.  So the tuner sweeps
+
+* the engine: "grid" or "cta";
+* the grid of the "grid" engine: 1/4, 1/2, 3/4 and all of the resident CTAs
+  (SMs x CTAs per SM);
+
+on a few full-graph searches of the job's own long nets over the current
+costs, and keeps the fastest.  Every setting returns the same paths (the
+searches are exact and independent of the schedule), so tuning changes only
+time.  Results are cached per (lattice, GPU) in a JSON file.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import json
+import os
+from dataclasses import asdict, dataclass, field
+from typing import Dict, List, Sequence, Tuple
+
+import torch
+
+from . import _lib
+
+
+@dataclass
+class Tuning:
+    key: str
+    full_engine: str
+    full_ctas: int
+    ms_per_search: Dict[str, float] = field(default_factory=dict)
+    samples: int = 0
+    cached: bool = False
+
+
+def full_grid(ctas: int = 0) -> Tuple[int, int]:
+    """Set (ctas > 0) or read the whole-lattice search's grid: (current, limit)."""
+    cur, lim = C.c_int32(0), C.c_int32(0)
+    _lib.check(_lib.load().ogr_full_grid(int(ctas), C.byref(cur), C.byref(lim)), "ogr_full_grid")
+    return int(cur.value), int(lim.value)
+
+
+def cache_path() -> str:
+    return os.environ.get("ORTHOROUTE_GB300_TUNE_CACHE",
+                          os.path.join(os.path.expanduser("~"), ".cache", "orthoroute_gb300", "autotune.json"))
+
+
+def lattice_key(lattice, device) -> str:
+    props = torch.cuda.get_device_properties(device)
+    spans = getattr(lattice, "allowed_via_spans", None)
+    spans = "all" if spans is None else ",".join(f"{a}-{b}" for a, b in sorted(spans))
+    return f"{props.name}/{props.multi_processor_count}sm/{lattice.nx}x{lattice.ny}x{lattice.nz}/{spans}"
+
+
+def _load_cache(path: str) -> Dict:
+    try:
+        with open(path) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+def _store_cache(path: str, key: str, t: Tuning) -> None:
+    data = _load_cache(path)
+    data[key] = asdict(t)
+    try:
+        os.makedirs(os.path.dirname(path), exist_ok=True)
+        tmp = f"{path}.{os.getpid()}.tmp"
+        with open(tmp, "w") as f:
+            json.dump(data, f, indent=1, sort_keys=True)
+        os.replace(tmp, path)
+    except OSError:
+        pass    # a read-only home only loses the cache
+
+
+def candidates(limit: int) -> List[Tuple[str, int]]:
+    grids = sorted({max(1, (limit * k) // 4) for k in (1, 2, 3, 4)})
+    return [("grid", c) for c in grids] + [("cta", 0)]
+
+
+def tune(ops, lattice, nets: Sequence[Tuple[int, int]], *, use_cache: bool = True, cta_max_nodes: int = 400_000,
+         repeats: int = 1) -> Tuning:
+    """Pick the engine and grid for full-graph searches of `lattice` by timing
+    searches of `nets` ((src, dst) pairs, full-graph length) on `ops`'s
+    current costs.  Leaves the chosen grid set and returns the choice."""
+    key = lattice_key(lattice, ops.g.device)
+    path = cache_path()
+    if use_cache:
+        hit = _load_cache(path).get(key)
+        if hit:
+            t = Tuning(**{**hit, "cached": True})
+            if t.full_engine == "grid":
+                full_grid(t.full_ctas)
+            return t
+    cur, limit = full_grid(0)
+    nets = list(nets)
+    timings: Dict[str, float] = {}
+    best = ("grid", limit, float("inf"))
+    stream = torch.cuda.current_stream()
+    if not nets:
+        return Tuning(key=key, full_engine="grid", full_ctas=cur)
+    # one untimed search first: workspace, lazy module load and caches
+    s0, d0 = nets[0]
+    ops.find_path(ops.net_args(0, s0, d0, full_graph=True, penalty=False), engine="grid")
+    try:
+        for engine, ctas in candidates(limit):
+            if engine == "cta" and ops.g.N > cta_max_nodes:
+                continue        # one CTA over a lattice this large is never the faster engine
+            if engine == "grid":
+                full_grid(ctas)
+            ms = 0.0
+            for _ in range(repeats):
+                for s, d in nets:
+                    net = ops.net_args(0, s, d, full_graph=True, penalty=False)
+                    t0 = ops.counters["search_ms"]
+                    ops.find_path(net, engine=engine)
+                    ms += ops.counters["search_ms"] - t0
+            ms /= max(1, repeats * len(nets))
+            name = f"grid{ctas}" if engine == "grid" else "cta"
+            timings[name] = round(ms, 4)
+            if ms < best[2]:
+                best = (engine, ctas, ms)
+    finally:
+        stream.synchronize()
+    engine, ctas, _ = best
+    full_grid(ctas if engine == "grid" else cur)
+    t = Tuning(key=key, full_engine=engine, full_ctas=ctas if engine == "grid" else cur, ms_per_search=timings,
+               samples=len(nets))
+    if use_cache:
+        _store_cache(path, key, t)
+    return t
+
+
+def sample_full_nets(tasks: Dict, distance, threshold: int, k: int = 3) -> List[Tuple[int, int]]:
+    """The k longest full-graph nets of a job (ties by name), for timing."""
+    rows = []
+    for name, (s, d) in tasks.items():
+        dist = distance(s, d)
+        if dist >= threshold:
+            rows.append((-dist, str(name), s, d))
+    rows.sort()
+    return [(s, d) for _, _, s, d in rows[:k]]

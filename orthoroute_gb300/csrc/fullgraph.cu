@@ -522,7 +522,21 @@ full_sssp_kernel(ogr_graph g, ogr_state st, ogr_full::Job job, FWs w) {
 }
 
 constexpr int kMaxDevices = 64;
-int g_grid_blocks[kMaxDevices] = {};
+int g_grid_blocks[kMaxDevices] = {};   // grid of the cooperative launch (0: not sized yet)
+int g_grid_limit[kMaxDevices] = {};    // SMs x resident CTAs per SM
+
+int size_grid(int dev) {
+  if (g_grid_limit[dev] == 0) {
+    int sms = 0, per_sm = 0, coop = 0;
+    OGR_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    OGR_CUDA_TRY(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
+    OGR_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, full_sssp_kernel, kThreads, 0));
+    if (!coop || per_sm < 1) return OGR_ERR_CUDA;
+    g_grid_limit[dev] = sms * per_sm;
+  }
+  if (g_grid_blocks[dev] == 0) g_grid_blocks[dev] = g_grid_limit[dev];
+  return OGR_OK;
+}
 
 }  // namespace
 
@@ -542,14 +556,8 @@ int launch(const ogr_graph& g, const ogr_state& st, const Job& job, void* ws, cu
   int dev = 0;
   OGR_CUDA_TRY(cudaGetDevice(&dev));
   if (dev < 0 || dev >= kMaxDevices) return OGR_ERR_ARG;
-  if (g_grid_blocks[dev] == 0) {
-    int sms = 0, per_sm = 0, coop = 0;
-    OGR_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    OGR_CUDA_TRY(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
-    OGR_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, full_sssp_kernel, kThreads, 0));
-    if (!coop || per_sm < 1) return OGR_ERR_CUDA;
-    g_grid_blocks[dev] = sms * per_sm;
-  }
+  const int rc = size_grid(dev);
+  if (rc != OGR_OK) return rc;
   FWs w;
   fws_layout(g.num_nodes, g.num_edges, (char*)ws, &w);
   // bar_count, bar_gen and bar_err start at zero on every launch
@@ -564,6 +572,19 @@ int launch(const ogr_graph& g, const ogr_state& st, const Job& job, void* ws, cu
 }
 
 }  // namespace ogr_full
+
+extern "C" int ogr_full_grid(int32_t ctas, int32_t* current, int32_t* limit) {
+  int dev = 0;
+  OGR_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kMaxDevices) return OGR_ERR_ARG;
+  const int rc = size_grid(dev);
+  if (rc != OGR_OK) return rc;
+  if (ctas < 0 || ctas > g_grid_limit[dev]) return OGR_ERR_ARG;
+  if (ctas > 0) g_grid_blocks[dev] = ctas;
+  if (current) *current = g_grid_blocks[dev];
+  if (limit) *limit = g_grid_limit[dev];
+  return OGR_OK;
+}
 
 extern "C" size_t ogr_full_workspace_bytes(int32_t num_nodes, int64_t num_edges) {
   return ogr_full::workspace_bytes(num_nodes, num_edges);

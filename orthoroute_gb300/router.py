@@ -265,21 +265,24 @@ class _PathDict(dict):
 
 
 class _FlatPaths:
-    """Every path of two or more nodes of one ``net_paths`` version,
-    concatenated in dict order.  ``owner[i]`` is the position in ``names`` of
-    the net of node i, ``ids`` the nets' router ids, ``hops`` the positions i
-    where (i, i+1) is a via hop of one net (same (x, y), different z)."""
+    """Every non-empty path of one ``net_paths`` version, concatenated in dict
+    order (one-node paths are the reference's trivially routed nets).
+    ``owner[i]`` is the position in ``names`` of the net of node i, ``ids``
+    the nets' router ids (-1 for a one-node path that never got one),
+    ``same[i]`` whether nodes i and i+1 are one net's hop, ``hops`` the
+    positions i where (i, i+1) is a via hop (same (x, y), different z)."""
 
-    def __init__(self, paths: _PathDict, plane: int, net_id):
+    def __init__(self, paths: _PathDict, plane: int, net_id, known_id):
         self.version = paths.version
         self.plane = plane
-        self.names = [n for n, p in paths.items() if p is not None and len(p) >= 2]
+        self.names = [n for n, p in paths.items() if p is not None and len(p) >= 1]
         arrs = [paths.array(n) for n in self.names]
         k = len(arrs)
         self.lens = np.fromiter((a.size for a in arrs), dtype=np.int64, count=k)
         self.nodes = np.concatenate(arrs) if k else np.zeros(0, dtype=np.int64)
         self.owner = np.repeat(np.arange(k, dtype=np.int64), self.lens)
-        self.ids = np.fromiter((net_id(n) for n in self.names), dtype=np.int64, count=k)
+        self.ids = np.fromiter((net_id(n) if a.size >= 2 else known_id(n) for n, a in zip(self.names, arrs)),
+                               dtype=np.int64, count=k)
         self.z, self.r = np.divmod(self.nodes, plane)
         self.same = self.owner[:-1] == self.owner[1:]
         self.hops = np.flatnonzero(self.same & (self.r[:-1] == self.r[1:]) & (self.z[:-1] != self.z[1:]))
@@ -382,12 +385,15 @@ class PathFinderRouter:
         require_cuda()
         if mode not in ("persistent", "plain"):
             raise ValueError("mode must be 'persistent' (one launch per routing pass) or 'plain' (one per net)")
-        if full_engine not in ("grid", "cta"):
-            raise ValueError("full_engine must be 'grid' (all SMs per full-graph net) or 'cta' (one CTA)")
+        if full_engine not in ("grid", "cta", "auto"):
+            raise ValueError("full_engine must be 'grid' (all SMs per full-graph net), 'cta' (one CTA) or "
+                             "'auto' (the autotuner picks per lattice)")
         self.config = config or PathFinderConfig()
         self.device = device
         self.mode = mode
         self.full_engine = full_engine
+        self.full_engine_request = full_engine
+        self.tuning = None
         self.window_slots = int(window_slots)   # > 0: batched disjoint-ROI windows in persistent mode
         self.store: Optional[PathStore] = None
         self.lattice: Optional[Lattice] = None
@@ -492,6 +498,9 @@ class PathFinderRouter:
     def initialize_lattice(self, lattice: Lattice, bounds=None, layer_names: Optional[List[str]] = None):
         """Build the device CSR and congestion state for a lattice."""
         self.lattice = lattice
+        self.tuning = None
+        if self.full_engine_request == "auto":
+            self.full_engine = "grid"
         # copper layer names as initialize_graph derives them (:2883-2904)
         names = list(layer_names) if layer_names else list(getattr(self.config, "layer_names", []) or [])
         if len(names) != lattice.nz:
@@ -661,7 +670,7 @@ class PathFinderRouter:
         """The flat view of the current paths (rebuilt after any change)."""
         f = self._flat_view
         if f is None or f.version != self._net_paths.version or f.src is not self._net_paths:
-            f = _FlatPaths(self._net_paths, self.plane, self._net_id)
+            f = _FlatPaths(self._net_paths, self.plane, self._net_id, lambda n: self.net_id_map.get(n, -1))
             f.src = self._net_paths
             self._flat_view = f
         return f
@@ -953,6 +962,15 @@ class PathFinderRouter:
             ordered = ordered[rotation:] + ordered[:rotation]
         return ordered
 
+    def _autotune(self, tasks):
+        """full_engine="auto": time the job's longest full-graph nets on the
+        current costs under each engine / grid and keep the fastest (the
+        choice changes no result)."""
+        from . import autotune
+        nets = autotune.sample_full_nets(tasks, self._manhattan, ROI_THRESHOLD_STEPS)
+        self.tuning = autotune.tune(self.ops, self.lattice, nets)
+        self.full_engine = self.tuning.full_engine
+
     def _route_all(self, tasks, all_tasks):
         cfg = self.config
         self.full_graph_fallback_count = 0
@@ -961,6 +979,8 @@ class PathFinderRouter:
         live = bool(cfg.live_present_costs)
         if live:
             self.ops.live_begin(self._present_pres_fac)
+        if self.full_engine_request == "auto" and self.tuning is None:
+            self._autotune(all_tasks)
         if self.mode == "persistent":
             return self._route_all_pass(tasks, all_tasks, ordered, bonus, live)
         for name in ordered:
@@ -1252,7 +1272,23 @@ class PathFinderRouter:
                 continue
             edges = self._apply(n, p, +1, live=False)
             self._update_tracking(n, edges)
+        self._add_trivial_use()
         self._rebuild_via_usage()
+
+    def _add_trivial_use(self):
+        """Path-node use of the trivially routed one-node nets.  The reference
+        rebuilds path_node_use from every path at the start of each iteration
+        (``_rebuild_via_usage_from_committed`` :4614-4615 via
+        ``_rebuild_path_node_use`` :4623-4633), so those nets count from
+        iteration 1 on; commits and rip-ups keep the rest up to date."""
+        single = [p[0] for p in self.net_paths.values() if p and len(p) == 1]
+        if not single:
+            return
+        idx = np.asarray(single, dtype=np.int64)
+        np.add.at(self.node_use, idx, 1)
+        use = self.s.path_node_use
+        use.index_add_(0, torch.from_numpy(idx).to(use.device),
+                       torch.ones(idx.size, dtype=use.dtype, device=use.device))
 
     def _rebuild_via_usage(self):
         self.pools.rebuild(self._flat())
@@ -1326,18 +1362,42 @@ class PathFinderRouter:
 
     # ------------------------------------------------------------- public API
     def _parse_requests(self, requests):
+        """``_parse_requests`` (:4386-4467) for ``(name, src, dst)`` tuples:
+        src == dst is routed trivially (``net_paths[name] = [src]``, no task);
+        endpoints that are not Python ints are skipped, as the reference skips
+        them.  Nets given by pads need the reference's pad portals, which this
+        router does not plan, so they raise."""
         tasks = {}
         for r in requests:
             if isinstance(r, tuple) and len(r) == 3:
-                tasks[str(r[0])] = (int(r[1]), int(r[2]))
-            else:
-                raise TypeError("requests must be (name, src_node, dst_node) tuples")
+                name, src, dst = r
+                if isinstance(src, int) and isinstance(dst, int):
+                    if src != dst:
+                        tasks[name] = (src, dst)
+                    else:
+                        self.net_paths[name] = [src]
+            elif hasattr(r, "name") and hasattr(r, "pads"):
+                raise TypeError("nets given by pads need pad portals; pass (name, src_node, dst_node) tuples")
         return tasks
+
+    @staticmethod
+    def _no_routable_nets(requests) -> Dict:
+        """The reference's result when no request yields a task (:4355-4381)."""
+        if not requests:
+            return {}
+        ids = [str(getattr(r, "name", r[0] if isinstance(r, tuple) and r else "unknown")) for r in requests]
+        return {'success': False, 'converged': False, 'nets_routed': 0, 'total_nets': len(requests),
+                'iterations': 0, 'total_time_s': 0.0, 'iteration_metrics': [], 'failed_nets': len(requests),
+                'overuse_sum': 0, 'overuse_edges': 0, 'barrel_conflicts': 0, 'excluded_nets': len(requests),
+                'excluded_net_ids': ids, 'error_code': 'NO-ROUTABLE-NETS',
+                'message': 'No routable nets were produced from the requests'}
 
     def route_multiple_nets(self, requests, progress_cb=None, iteration_cb=None) -> Dict:
         if self.lattice is None:
             raise RuntimeError("initialize_graph() first")
         tasks = self._parse_requests(requests)
+        if not tasks:
+            return self._no_routable_nets(requests)
         self._tasks_all = tasks
         self._task_names = list(tasks)
         self._task_index = {n: i for i, n in enumerate(self._task_names)}
@@ -1350,6 +1410,7 @@ class PathFinderRouter:
         self._indices_host = self.g.indices.cpu().numpy()
         self._edge_layer_host = self.g.edge_layer.cpu().numpy()
         self._edge_kind_host = self.g.edge_kind.cpu().numpy().astype(bool)
+        self._add_trivial_use()
         return self._negotiate(tasks, progress_cb, iteration_cb)
 
     def _derive(self, tasks):

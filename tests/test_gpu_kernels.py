@@ -390,3 +390,49 @@ def test_apply_path_node_state_matches_oracle():
     ns.clear_use(paths[2])
     np.testing.assert_array_equal(owner(), ns.owner)
     np.testing.assert_array_equal(s.path_node_use.cpu().numpy(), ns.path_node_use.astype(np.int32))
+
+
+@pytest.mark.parametrize("quarter", [1, 2, 3])
+def test_full_grid_search_any_grid_size(quarter):
+    """The autotuner's grid sizes: the same paths and statistics on 1/4 .. 3/4 of the CTAs."""
+    from orthoroute_gb300.autotune import full_grid
+    g, s, ops, ref = make(120, 90, 8)
+    rng = np.random.default_rng(500 + quarter)
+    costs = _costs(quarter, g.E, rng)
+    s.total_cost.copy_(torch.from_numpy(costs))
+    ident = np.arange(g.N, dtype=np.int32)
+    cur, lim = full_grid(0)
+    try:
+        full_grid(max(1, lim * quarter // 4))
+        for _ in range(3):
+            src, dst = (int(v) for v in rng.integers(0, ref.plane, size=2))
+            st = {}
+            want = find_path_roi_c(ref.indptr, ref.indices, src, dst, costs, ident, ident, stats=st)
+            ops.stats.zero_()
+            got = ops.find_path(ops.net_args(0, src, dst, full_graph=True, penalty=False), engine="grid")
+            assert got == want
+            if want is not None:
+                assert ops.stats.cpu().tolist()[:2] == [st["scanned"], st["settled"]]
+    finally:
+        full_grid(cur)
+
+
+def test_autotune_times_every_candidate(tmp_path, monkeypatch):
+    from orthoroute_gb300 import Lattice, autotune
+    monkeypatch.setenv("ORTHOROUTE_GB300_TUNE_CACHE", str(tmp_path / "tune.json"))
+    g, s, ops, ref = make(200, 60, 6)
+    s.total_cost.copy_(torch.from_numpy(_costs(3, g.E, np.random.default_rng(1))))
+    cur, lim = autotune.full_grid(0)
+    lat = Lattice(200, 60, 6)
+    nets = [(2, 60 * 200 - 3), (200 * 30 + 1, 200 * 31 - 2)]
+    try:
+        t = autotune.tune(ops, lat, nets)
+        assert not t.cached and t.samples == 2
+        assert set(t.ms_per_search) == {f"grid{c}" for _, c in autotune.candidates(lim)[:-1]} | {"cta"}
+        assert t.full_engine in ("grid", "cta")
+        if t.full_engine == "grid":
+            assert autotune.full_grid(0)[0] == t.full_ctas
+        t2 = autotune.tune(ops, lat, nets)
+        assert t2.cached and (t2.full_engine, t2.full_ctas) == (t.full_engine, t.full_ctas)
+    finally:
+        autotune.full_grid(cur)

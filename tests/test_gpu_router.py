@@ -78,12 +78,13 @@ def seeded_nets(nx, ny, n, seed, dmin=5, dmax=80):
 
 CASES = [((40, 36, 6), 60, 8, 7, 160, "grid"), ((48, 40, 8), 90, 10, 11, 160, "grid"),
          ((140, 40, 6), 40, 6, 5, 160, "grid"), ((140, 40, 6), 40, 6, 5, 160, "cta"),
-         ((260, 60, 8), 50, 6, 3, 300, "grid")]
+         ((260, 60, 8), 50, 6, 3, 300, "grid"), ((260, 60, 8), 50, 6, 3, 300, "auto")]
 
 
 @pytest.mark.parametrize("mode", ["persistent", "plain"])
 @pytest.mark.parametrize("dims,n_nets,iters,seed,dmax,engine", CASES)
-def test_gpu_router_matches_oracle_loop(dims, n_nets, iters, seed, dmax, engine, mode):
+def test_gpu_router_matches_oracle_loop(dims, n_nets, iters, seed, dmax, engine, mode, tmp_path, monkeypatch):
+    monkeypatch.setenv("ORTHOROUTE_GB300_TUNE_CACHE", str(tmp_path / "tune.json"))
     nx, ny, nz = dims
     reqs = seeded_nets(nx, ny, n_nets, seed, dmin=5, dmax=dmax)
     R = gpu_router(nx, ny, nz, iters, mode, engine)
@@ -99,3 +100,40 @@ def test_gpu_router_matches_oracle_loop(dims, n_nets, iters, seed, dmax, engine,
     for k in ("barrel_conflicts", "overuse_sum", "failed_nets"):
         if k in ores and k in res:
             assert res[k] == ores[k], k
+    if engine == "auto":
+        assert R.tuning is not None and R.full_engine == R.tuning.full_engine
+
+
+@pytest.mark.parametrize("mode", ["persistent", "plain"])
+def test_gpu_router_trivial_and_skipped_requests(mode):
+    """Requests with src == dst are routed trivially (a one-node path, no
+    task), non-int endpoints are skipped, as the reference parses them; the
+    run equals the oracle loop started with the trivial paths in place."""
+    nx, ny, nz, iters = 40, 36, 6, 6
+    reqs = seeded_nets(nx, ny, 50, 21, dmin=5, dmax=160)
+    trivial = [(f"N{50 + k}", reqs[k][1], reqs[k][1]) for k in range(0, 12, 3)]
+    skipped = [("N99", np.int64(5), 9)]
+    R = gpu_router(nx, ny, nz, iters, mode)
+    R.trace = []
+    res = R.route_multiple_nets(reqs + trivial + skipped)
+    assert "N99" not in R.net_paths
+    assert all(R.net_paths[n] == [s] for n, s, _ in trivial)
+    O = OracleRouter(LatticeSpec(nx, ny, nz), board_bounds(nx, ny), Config(max_iterations=iters), fast=True)
+    O.trace = []
+    for n, s, _ in trivial:
+        O.net_paths[n] = [s]
+    ores = O.route({n: (s, d) for n, s, d in reqs})
+    assert len(R.trace) == len(O.trace)
+    for j, (a, b) in enumerate(zip(R.trace, O.trace)):
+        np.testing.assert_array_equal(flat(a), flat(b), err_msg=f"record {j}")
+    for k in ("barrel_conflicts", "overuse_sum", "failed_nets"):
+        if k in ores and k in res:
+            assert res[k] == ores[k], k
+
+
+def test_gpu_router_no_routable_nets():
+    R = gpu_router(20, 16, 6, 4)
+    assert R.route_multiple_nets([]) == {}
+    res = R.route_multiple_nets([("A", 7, 7), ("B", 3.0, 9)])
+    assert res["error_code"] == "NO-ROUTABLE-NETS" and res["excluded_net_ids"] == ["A", "B"]
+    assert res["failed_nets"] == 2 and not res["success"]
