@@ -8,7 +8,7 @@ resident in HBM; ``e2e`` is the same job through the public router API
 starting from host requests (CSR build, state upload and the path read-back
 inside the timed region).
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--config c1|c0]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--config c1|c0|c2|c4]
                     [--impl ours|reference]
 
 ``--impl reference`` times the CPU restatement of the reference's routing
@@ -42,6 +42,10 @@ CONFIGS = {
                plain_iters=1, plain_nets=200, searches_per_job=10364,
                # DRAM bytes / algorithmic bytes of full_sssp_kernel, ncu on a 300x200x8 search
                traffic_ratio=0.6655),
+    # BASELINE configs[2]: 600x400x12, 1,500 multi-pin nets (2-16 pins, 1 + geometric(0.35)) with
+    # pins inside a seeded 50x50 box per net, as star two-pin requests p0 -> pi (multipin.py)
+    "c2": dict(nx=600, ny=400, nz=12, nets=1500, iters=40, seed=2468, multipin=True, via_span=4,
+               plain_iters=1, plain_nets=300, searches_per_job=52476),
 }
 
 
@@ -87,8 +91,12 @@ def make_lattice(cfg):
 
 
 def make_requests(cfg):
-    """Seeded two-pin nets with endpoints on layer 0 (numpy default_rng)."""
+    """Seeded two-pin nets with endpoints on layer 0 (numpy default_rng); for a
+    multi-pin config, the star requests of seeded multi-pin nets."""
     nx, ny, n = cfg["nx"], cfg["ny"], cfg["nets"]
+    if cfg.get("multipin"):
+        from orthoroute_gb300.multipin import seeded_multipin_nets, star_requests
+        return star_requests(seeded_multipin_nets(nx, ny, n, cfg["seed"]))
     rng = np.random.default_rng(cfg["seed"])
     out = []
     if not cfg["clusters"]:
@@ -292,6 +300,9 @@ def run_ours(args, cfg, rank, world):
         "result": {k: res.get(k) for k in ("success", "converged", "iterations", "overuse_sum", "barrel_conflicts",
                                            "failed_nets")},
         "sssp_gteps": round(gteps, 4),
+        # device time of the search launches (CUDA events on the routing stream) vs the whole job
+        "time_split": {"search_kernels_s": round(search_ms / 1e3 / max(1, args.steps), 3),
+                       "job_s": round(ms / 1e3, 3)},
         "searches_per_job": prof["searches"] // max(1, args.steps),
         "roofline": {"bound": "hbm", "achieved": round(achieved, 3), "peak": pk.get("hbm_gbs"), "unit": "GB/s",
                      "frac": round(achieved / pk.get("hbm_gbs", 1.0), 6),
@@ -324,7 +335,7 @@ def run_ours(args, cfg, rank, world):
 
 
 # ---------------------------------------------------------------- CPU baseline
-def cpu_job_sample(cfg, budget_s=20.0):
+def cpu_job_sample(cfg, budget_s=20.0, searches_hint=None):
     """Time the oracle (C heap Dijkstra core) on the job: full job when it
     fits the budget, else the first iterations, scaled by searches."""
     from oracle.lattice import LatticeSpec
@@ -348,7 +359,7 @@ def cpu_job_sample(cfg, budget_s=20.0):
     R.route(sample)
     dt = time.perf_counter() - t1
     per = dt / max(1, R.stats["searches"])
-    n = cfg["searches_per_job"]
+    n = cfg["searches_per_job"] or searches_hint
     return per * n, (f"{R.stats['searches']} searches of iteration 1 ({len(sample)} nets, {dt:.1f} s, "
                      f"{per:.3f} s/search) x {n} searches per job; host policy time excluded"), 1
 
@@ -440,7 +451,7 @@ def main():
         tdist.init_process_group("nccl")
     line = run_ours(args, cfg, rank, world)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        v, sample, cores = cpu_job_sample(cfg)
+        v, sample, cores = cpu_job_sample(cfg, searches_hint=line["searches_per_job"])
         line["cpu_baseline"] = {"value": round(v, 4), "unit": "s/job", "cores": cores, "kind": "port",
                                 "sample": sample}
     if rank == 0:

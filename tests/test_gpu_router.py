@@ -137,3 +137,28 @@ def test_gpu_router_no_routable_nets():
     res = R.route_multiple_nets([("A", 7, 7), ("B", 3.0, 9)])
     assert res["error_code"] == "NO-ROUTABLE-NETS" and res["excluded_net_ids"] == ["A", "B"]
     assert res["failed_nets"] == 2 and not res["success"]
+
+
+@pytest.mark.parametrize("mode", ["persistent", "plain"])
+def test_gpu_router_multipin_star_matches_oracle_loop(mode):
+    """Multi-pin nets (2-16 pins in a box) as star requests: every sink of every
+    net in the persistent pass, paths identical to the oracle loop's."""
+    from orthoroute_gb300.multipin import seeded_multipin_nets, star_requests
+    nx, ny, nz, iters = 60, 50, 6, 6
+    reqs = star_requests(seeded_multipin_nets(nx, ny, 25, 8, box=20))
+    R = gpu_router(nx, ny, nz, iters, mode)
+    R.trace = []
+    res = R.route_multiple_nets(reqs)
+    O = OracleRouter(LatticeSpec(nx, ny, nz), board_bounds(nx, ny), Config(max_iterations=iters), fast=True)
+    O.trace = []
+    for n, s, d in reqs:
+        if s == d:
+            O.net_paths[n] = [s]
+    ores = O.route({n: (s, d) for n, s, d in reqs if s != d})
+    key = lambda paths: {k: list(v) for k, v in paths.items()}
+    assert len(R.trace) == len(O.trace)
+    for j, (a, b) in enumerate(zip(R.trace, O.trace)):
+        assert key(a) == key(b), f"record {j}"
+    for k in ("barrel_conflicts", "overuse_sum", "failed_nets"):
+        if k in ores and k in res:
+            assert res[k] == ores[k], k
