@@ -323,7 +323,8 @@ def run_ours(args, cfg, rank, world):
         "mode": args.mode,
         "full_engine": {"requested": args.full_engine, "used": router.full_engine,
                         "tuning": (None if router.tuning is None else
-                                   {"ctas": router.tuning.full_ctas, "ms_per_search": router.tuning.ms_per_search,
+                                   {"ctas": router.tuning.full_ctas, "roi_lanes": router.tuning.roi_lanes,
+                                    "ms_per_search": router.tuning.ms_per_search,
                                     "cached": router.tuning.cached})},
     }
     if plain is not None:

@@ -384,6 +384,12 @@ int ogr_find_path_full(const ogr_graph* g, const ogr_state* st, const ogr_net_ar
  * (orthoroute_gb300/autotune.py); no reference counterpart. */
 int ogr_full_grid(int32_t ctas, int32_t* current, int32_t* limit);
 
+/* Lanes per node of the single-CTA ROI search (2, 4, 8 or 16; default 4) for
+ * every search launched afterwards; 0 only reads.  *current (host, may be
+ * NULL) receives the setting.  A tuning knob (results do not depend on it),
+ * process-wide, chosen by the autotuner; no reference counterpart. */
+int ogr_search_lanes(int32_t lanes, int32_t* current);
+
 /* Tracing of the whole-lattice search (host int64[8], cumulative since the
  * last reset): searches, phases, kernel ns, init ns, E-step work ns and
  * S-step work ns of the busiest CTA, barrier wait ns and statistics +

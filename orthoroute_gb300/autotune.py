@@ -1,4 +1,4 @@
-"""Autotuner for the whole-lattice search: engine and CTA grid per lattice size.
+"""Autotuner: search engine, CTA grid and lanes per node, per lattice size.
 
 Full-graph nets (Manhattan length >= 125, ``_route_all`` :8219-8262) are
 searched either by ``full_sssp_kernel`` on a cooperative grid of CTAs (one
@@ -14,9 +14,13 @@ settle rule is fixed by exactness.  So the tuner sweeps
   (SMs x CTAs per SM);
 
 on a few full-graph searches of the job's own long nets over the current
-costs, and keeps the fastest.  Every setting returns the same paths (the
-searches are exact and independent of the schedule), so tuning changes only
-time.  Results are cached per (lattice, GPU) in a JSON file.
+costs, and keeps the fastest.  For ROI nets (one 1024-thread CTA per search)
+it sweeps the lanes that serve one node (2, 4, 8, 16: the CTA's tile of
+nodes in flight is 1024 / lanes), timing a spread of the job's ROI nets; the
+best width follows the lattice's arcs per node.  Every setting returns the
+same paths (the searches are exact and independent of the schedule), so
+tuning changes only time.  Results are cached per (lattice, GPU) in a JSON
+file.
 """
 from __future__ import annotations
 
@@ -37,6 +41,7 @@ class Tuning:
     full_engine: str
     full_ctas: int
     ms_per_search: Dict[str, float] = field(default_factory=dict)
+    roi_lanes: int = 4
     samples: int = 0
     cached: bool = False
 
@@ -46,6 +51,16 @@ def full_grid(ctas: int = 0) -> Tuple[int, int]:
     cur, lim = C.c_int32(0), C.c_int32(0)
     _lib.check(_lib.load().ogr_full_grid(int(ctas), C.byref(cur), C.byref(lim)), "ogr_full_grid")
     return int(cur.value), int(lim.value)
+
+
+def search_lanes(lanes: int = 0) -> int:
+    """Set (lanes > 0) or read the ROI search's lanes per node."""
+    cur = C.c_int32(0)
+    _lib.check(_lib.load().ogr_search_lanes(int(lanes), C.byref(cur)), "ogr_search_lanes")
+    return int(cur.value)
+
+
+LANES = (2, 4, 8, 16)
 
 
 def cache_path() -> str:
@@ -86,11 +101,20 @@ def candidates(limit: int) -> List[Tuple[str, int]]:
     return [("grid", c) for c in grids] + [("cta", 0)]
 
 
-def tune(ops, lattice, nets: Sequence[Tuple[int, int]], *, use_cache: bool = True, cta_max_nodes: int = 400_000,
-         repeats: int = 1) -> Tuning:
+def _time_roi(ops, nets, lanes) -> float:
+    search_lanes(lanes)
+    t0 = ops.counters["search_ms"]
+    for s, d in nets:
+        ops.find_path(ops.net_args(0, s, d, full_graph=False, penalty=False), engine="cta")
+    return (ops.counters["search_ms"] - t0) / max(1, len(nets))
+
+
+def tune(ops, lattice, nets: Sequence[Tuple[int, int]], roi_nets: Sequence[Tuple[int, int]] = (), *,
+         use_cache: bool = True, cta_max_nodes: int = 400_000, repeats: int = 1) -> Tuning:
     """Pick the engine and grid for full-graph searches of `lattice` by timing
-    searches of `nets` ((src, dst) pairs, full-graph length) on `ops`'s
-    current costs.  Leaves the chosen grid set and returns the choice."""
+    searches of `nets` ((src, dst) pairs, full-graph length), and the lanes
+    per node of ROI searches by timing `roi_nets`, on `ops`'s current costs.
+    Leaves the choices set and returns them."""
     key = lattice_key(lattice, ops.g.device)
     path = cache_path()
     if use_cache:
@@ -99,14 +123,28 @@ def tune(ops, lattice, nets: Sequence[Tuple[int, int]], *, use_cache: bool = Tru
             t = Tuning(**{**hit, "cached": True})
             if t.full_engine == "grid":
                 full_grid(t.full_ctas)
+            search_lanes(t.roi_lanes)
             return t
     cur, limit = full_grid(0)
     nets = list(nets)
+    roi_nets = list(roi_nets)
     timings: Dict[str, float] = {}
+    lanes0 = search_lanes(0)
+    best_lanes = lanes0
+    if roi_nets:
+        _time_roi(ops, roi_nets[:1], lanes0)       # untimed: workspace and caches
+        lane_ms = {lanes: _time_roi(ops, roi_nets, lanes) for lanes in LANES}
+        best_lanes = min(LANES, key=lambda k: (lane_ms[k], k))
+        timings.update({f"roi_lanes{k}": round(v, 4) for k, v in lane_ms.items()})
+    search_lanes(best_lanes)
     best = ("grid", limit, float("inf"))
     stream = torch.cuda.current_stream()
     if not nets:
-        return Tuning(key=key, full_engine="grid", full_ctas=cur)
+        t = Tuning(key=key, full_engine="grid", full_ctas=cur, ms_per_search=timings, roi_lanes=best_lanes,
+                   samples=len(roi_nets))
+        if use_cache:
+            _store_cache(path, key, t)
+        return t
     # one untimed search first: workspace, lazy module load and caches
     s0, d0 = nets[0]
     ops.find_path(ops.net_args(0, s0, d0, full_graph=True, penalty=False), engine="grid")
@@ -133,10 +171,19 @@ def tune(ops, lattice, nets: Sequence[Tuple[int, int]], *, use_cache: bool = Tru
     engine, ctas, _ = best
     full_grid(ctas if engine == "grid" else cur)
     t = Tuning(key=key, full_engine=engine, full_ctas=ctas if engine == "grid" else cur, ms_per_search=timings,
-               samples=len(nets))
+               samples=len(nets) + len(roi_nets), roi_lanes=best_lanes)
     if use_cache:
         _store_cache(path, key, t)
     return t
+
+
+def sample_roi_nets(tasks: Dict, distance, threshold: int, k: int = 16) -> List[Tuple[int, int]]:
+    """Up to k ROI nets of a job spread evenly over its name order, for timing."""
+    rows = sorted((str(n), s, d) for n, (s, d) in tasks.items() if 0 < distance(s, d) < threshold)
+    if not rows:
+        return []
+    step = max(1, len(rows) // k)
+    return [(s, d) for _, s, d in rows[::step][:k]]
 
 
 def sample_full_nets(tasks: Dict, distance, threshold: int, k: int = 3) -> List[Tuple[int, int]]:

@@ -42,8 +42,27 @@ namespace {
 
 constexpr int kThreads = 1024;
 constexpr int kWarps = kThreads / 32;
-constexpr int kSub = 16;                       // lanes per node
-constexpr int kGroups = kThreads / kSub;       // nodes in flight per CTA
+constexpr int kSub = 16;                       // lanes per node (ROI BFS)
+constexpr int kGroups = kThreads / kSub;       // nodes in flight per CTA (ROI BFS)
+#ifndef OGR_SEARCH_LANES
+#define OGR_SEARCH_LANES 4
+#endif
+constexpr int kSearchLanes = OGR_SEARCH_LANES;  // default lanes per node of the ROI search
+
+// Lanes per node of the ROI search for the launches that follow (set by
+// ogr_search_lanes; the autotuner picks it per lattice).  Every searching
+// kernel exists for 2, 4, 8 and 16 lanes; results do not depend on the choice.
+int g_search_lanes = kSearchLanes;
+
+#define OGR_WITH_LANES(LV, ...)                                \
+  do {                                                         \
+    switch (g_search_lanes) {                                  \
+      case 2: { constexpr int LV = 2; __VA_ARGS__; } break;    \
+      case 8: { constexpr int LV = 8; __VA_ARGS__; } break;    \
+      case 16: { constexpr int LV = 16; __VA_ARGS__; } break;  \
+      default: { constexpr int LV = 4; __VA_ARGS__; } break;   \
+    }                                                          \
+  } while (0)
 constexpr int32_t ST_NONE = 0, ST_FRONT = 1, ST_DONE = 2, ST_SINK = 3;  // SINK: a settled target (multi-seed)
 constexpr int kMaxViaNodes = 4096;
 constexpr int kDMax = 32;                      // arcs per node the local adjacency holds
@@ -434,11 +453,19 @@ __device__ void roi_build(Shared& sh, const ogr_graph& g, const ogr_net_args& a,
 // expanded, the search runs until nothing is left, and the result is the
 // settled target with the least (label + target cost), first in pop order
 // (label, ROI index) among equals.
-template <bool kMulti = false>
+//
+// kLanes lanes serve one node (its arcs, then a shuffle reduction), so a CTA
+// keeps 1024 / kLanes nodes in flight per round of a phase.
+template <bool kMulti = false, int kLanes = kSearchLanes>
 __device__ void sssp_roi(Shared& sh, const ogr_graph& g, const ogr_state& st, const ogr_net_args& a, const Ws& w,
                          const int32_t* roi, int32_t R, int32_t* path_out, int32_t path_cap,
                          unsigned long long* stats_acc, StageClock& clk, const float* roi_pen = nullptr,
                          const MultiSeeds* ms = nullptr) {
+  static_assert(kLanes == 2 || kLanes == 4 || kLanes == 8 || kLanes == 16 || kLanes == 32,
+                "lanes per node: a power of two from 2 to 32");
+  constexpr int kSub = kLanes;                  // shadows the BFS's lane count inside the search
+  constexpr int kGroups = kThreads / kLanes;
+  constexpr int kPerWarp = 32 / kLanes;
   const int tid = threadIdx.x;
   const int lane = tid & 31, warp = tid >> 5;
   const int sl = tid & (kSub - 1), grp = tid / kSub;
@@ -501,16 +528,12 @@ __device__ void sssp_roi(Shared& sh, const ogr_graph& g, const ogr_state& st, co
       const int32_t rg = roi[r];
       const int32_t e0 = indptr[rg], e1 = indptr[rg + 1];
       if (e1 - e0 > kDMax) too_wide = 1;
-      for (int k = sl; k < kDMax; k += kSub) {
+      // only the node's own arcs: slots past its degree are never read
+      const int dr = min(e1 - e0, kDMax);
+      for (int k = sl; k < dr; k += kSub) {
         const int32_t e = e0 + k;
-        int32_t u = -1;
-        float c = kInf;
-        if (e < e1) {
-          u = w.g2r[indices[e]];
-          c = st.rcost ? st.rcost[e] : st.total_cost[g.rev[e]];
-        }
-        w.adj[(int64_t)r * kDMax + k] = u;
-        w.acost[(int64_t)r * kDMax + k] = c;
+        w.adj[(int64_t)r * kDMax + k] = w.g2r[indices[e]];
+        w.acost[(int64_t)r * kDMax + k] = st.rcost ? st.rcost[e] : st.total_cost[g.rev[e]];
       }
       if (sl == 0) w.deg[r] = min(e1 - e0, kDMax);
     }
@@ -578,10 +601,10 @@ __device__ void sssp_roi(Shared& sh, const ogr_graph& g, const ogr_state& st, co
       __syncthreads();
       clk.mark(3);
       // 2. recompute each queued node from all settled in-neighbours: a
-      //    16-lane group per node, lanes over its arcs, shuffle reduction.
+      //    kLanes-lane group per node, lanes over its arcs, shuffle reduction.
       const int nd = sh.ndirty;
-      const int half = lane >> 4;
-      for (int base = warp * 2; base < nd; base += kWarps * 2) {
+      const int half = lane / kLanes;
+      for (int base = warp * kPerWarp; base < nd; base += kWarps * kPerWarp) {
         const int idx = base + half;
         const bool valid = idx < nd;
         const int32_t y = valid ? w.dl[idx] : 0;
@@ -592,7 +615,7 @@ __device__ void sssp_roi(Shared& sh, const ogr_graph& g, const ogr_state& st, co
           if (sl == 0)
             p = !fresh ? node[y].pen : (roi_pen ? roi_pen[y] : ogr_node_penalty(st, a, full ? y : roi[y]));
         }
-        p = __shfl_sync(0xffffffffu, p, lane & 16);
+        p = __shfl_sync(0xffffffffu, p, lane & ~(kLanes - 1));
         const double pd = (double)p;
         float ba = kInf, bc = kInf;
         double bl = 0.0;
@@ -647,7 +670,7 @@ __device__ void sssp_roi(Shared& sh, const ogr_graph& g, const ogr_state& st, co
           }
         }
 #pragma unroll
-        for (int o = 8; o > 0; o >>= 1) {
+        for (int o = kLanes / 2; o > 0; o >>= 1) {
           const float oa = __shfl_xor_sync(0xffffffffu, ba, o);
           const double ol = __shfl_xor_sync(0xffffffffu, bl, o);
           const int32_t ou = __shfl_xor_sync(0xffffffffu, bu, o);
@@ -850,6 +873,7 @@ __device__ void sssp_roi(Shared& sh, const ogr_graph& g, const ogr_state& st, co
 }
 
 // Whole search for one net on one CTA (ROI extraction inline).
+template <int L>
 __device__ void search_net(Shared& sh, const ogr_graph& g, const ogr_state& st, const ogr_net_args& a, const Ws& w,
                            int32_t* path_out, int32_t path_cap, unsigned long long* stats_acc) {
   StageClock clk;
@@ -866,7 +890,7 @@ __device__ void search_net(Shared& sh, const ogr_graph& g, const ogr_state& st, 
     R = sh.R;
   }
   if (sh.status != OGR_OK) return;
-  sssp_roi(sh, g, st, a, w, w.roi, R, path_out, path_cap, stats_acc, clk);
+  sssp_roi<false, L>(sh, g, st, a, w, w.roi, R, path_out, path_cap, stats_acc, clk);
 }
 
 // ---- commit / rip-up ---------------------------------------------------------
@@ -944,11 +968,12 @@ __device__ int apply_path_dev(const ogr_graph& g, const ogr_state& st, const int
 }
 
 // ---- kernels -------------------------------------------------------------------
+template <int L>
 __global__ void __launch_bounds__(kThreads, 1)
 find_path_kernel(ogr_graph g, ogr_state st, ogr_net_args a, Ws w, int32_t* path_out, int32_t path_cap,
                  int64_t* stats) {
   __shared__ Shared sh;
-  search_net(sh, g, st, a, w, path_out, path_cap, reinterpret_cast<unsigned long long*>(stats));
+  search_net<L>(sh, g, st, a, w, path_out, path_cap, reinterpret_cast<unsigned long long*>(stats));
   if (threadIdx.x == 0) {
     w.result[0] = sh.status;
     w.result[1] = sh.len;
@@ -957,6 +982,7 @@ find_path_kernel(ogr_graph g, ogr_state st, ogr_net_args a, Ws w, int32_t* path_
 
 // The reference's solver seam: search a given ROI (ROI order = tie order)
 // with a given ROI-local penalty array (or none).
+template <int L>
 __global__ void __launch_bounds__(kThreads, 1)
 find_path_given_roi_kernel(ogr_graph g, ogr_state st, ogr_net_args a, Ws w, const int32_t* roi, int32_t R,
                            const float* roi_pen, int32_t* path_out, int32_t path_cap, int64_t* stats) {
@@ -969,7 +995,8 @@ find_path_given_roi_kernel(ogr_graph g, ogr_state st, ogr_net_args a, Ws w, cons
     sh.found = 0;
   }
   __syncthreads();
-  sssp_roi(sh, g, st, a, w, roi, R, path_out, path_cap, reinterpret_cast<unsigned long long*>(stats), clk, roi_pen);
+  sssp_roi<false, L>(sh, g, st, a, w, roi, R, path_out, path_cap, reinterpret_cast<unsigned long long*>(stats), clk,
+                     roi_pen);
   if (threadIdx.x == 0) {
     w.result[0] = sh.status;
     w.result[1] = sh.len;
@@ -977,6 +1004,7 @@ find_path_given_roi_kernel(ogr_graph g, ogr_state st, ogr_net_args a, Ws w, cons
 }
 
 // The multi-source multi-sink seam on a given ROI.
+template <int L>
 __global__ void __launch_bounds__(kThreads, 1)
 find_path_multi_kernel(ogr_graph g, ogr_state st, ogr_net_args a, Ws w, const int32_t* roi, int32_t R,
                        const float* roi_pen, MultiSeeds ms, int32_t* path_out, int32_t path_cap, int64_t* stats) {
@@ -989,7 +1017,7 @@ find_path_multi_kernel(ogr_graph g, ogr_state st, ogr_net_args a, Ws w, const in
     sh.found = 0;
   }
   __syncthreads();
-  sssp_roi<true>(sh, g, st, a, w, roi, R, path_out, path_cap, reinterpret_cast<unsigned long long*>(stats), clk,
+  sssp_roi<true, L>(sh, g, st, a, w, roi, R, path_out, path_cap, reinterpret_cast<unsigned long long*>(stats), clk,
                  roi_pen, &ms);
   if (threadIdx.x == 0) {
     w.result[0] = sh.status;
@@ -1086,6 +1114,7 @@ roi_batch_kernel(ogr_graph g, ogr_net_table t, ogr_pass_args pa, ogr_roi_batch r
 }
 
 // One launch routes an ordered list of nets the way _route_all does.
+template <int L>
 __global__ void __launch_bounds__(kThreads, 1)
 route_pass_kernel(ogr_graph g, ogr_state st, ogr_net_table t, ogr_pass_args pa, ogr_roi_batch rb, int use_batch,
                   Ws w) {
@@ -1123,9 +1152,9 @@ route_pass_kernel(ogr_graph g, ogr_state st, ogr_net_table t, ogr_pass_args pa, 
         atomicAdd(&g_stage[14], 1ull);
       }
       __syncthreads();
-      sssp_roi(sh, g, st, a, w, rb.roi_pool + (int64_t)n * rb.roi_cap, pre, slot, t.slot_cap, stats, clk);
+      sssp_roi<false, L>(sh, g, st, a, w, rb.roi_pool + (int64_t)n * rb.roi_cap, pre, slot, t.slot_cap, stats, clk);
     } else {
-      search_net(sh, g, st, a, w, slot, t.slot_cap, stats);
+      search_net<L>(sh, g, st, a, w, slot, t.slot_cap, stats);
     }
     int flags = 0;
     const int st1 = sh.status;
@@ -1137,7 +1166,7 @@ route_pass_kernel(ogr_graph g, ogr_state st, ogr_net_table t, ogr_pass_args pa, 
       a = ogr_pass_net_args(t, pa, n, 1);
       __syncthreads();
       if (threadIdx.x == 0) ++s_fallbacks;
-      search_net(sh, g, st, a, w, slot, t.slot_cap, stats);
+      search_net<L>(sh, g, st, a, w, slot, t.slot_cap, stats);
       const int st2 = sh.status;
       if (st2 < 0) {
         if (threadIdx.x == 0) s_error = st2;
@@ -1257,6 +1286,7 @@ __device__ int commit_from(const ogr_graph& g, const ogr_state& st, const ogr_ne
 // into scratch; then either every net commits (no failure) or CTA 0 commits in
 // order up to the first failed net, undoes the later nets' rip-ups and runs
 // the failed net's fallback.
+template <int L>
 __global__ void __launch_bounds__(kThreads, 1)
 window_pass_kernel(ogr_graph g, ogr_state st, ogr_net_table t, ogr_pass_args pa, ogr_roi_batch rb, char* slot_base,
                    size_t slot_bytes, int32_t rmax, int32_t* scratch, char* ctl_base, Ws w) {
@@ -1337,13 +1367,14 @@ window_pass_kernel(ogr_graph g, ogr_state st, ogr_net_table t, ogr_pass_args pa,
       if (rc == OGR_OK) {
         const ogr_net_args a = ogr_pass_net_args(t, pa, n, 0);
         if (ws.solo[b]) {
-          search_net(sh, g, st, a, w, my_path, t.slot_cap, ws.stats + 4 * b);
+          search_net<L>(sh, g, st, a, w, my_path, t.slot_cap, ws.stats + 4 * b);
         } else {
           StageClock clk;
           clk.start();
           if (tid == 0) sh.status = OGR_OK;
           __syncthreads();
-          sssp_roi(sh, g, st, a, mine, rb.roi_pool + (int64_t)n * rb.roi_cap, rb.roi_len[n], my_path, t.slot_cap,
+          sssp_roi<false, L>(sh, g, st, a, mine, rb.roi_pool + (int64_t)n * rb.roi_cap, rb.roi_len[n], my_path,
+                             t.slot_cap,
                    ws.stats + 4 * b, clk);
         }
         if (tid == 0) {
@@ -1396,7 +1427,7 @@ window_pass_kernel(ogr_graph g, ogr_state st, ogr_net_table t, ogr_pass_args pa,
       const int used = (int)w.result[2];
       if (rc == OGR_OK && fin != OGR_OK && used < pa.fallback_quota) {
         const ogr_net_args a = ogr_pass_net_args(t, pa, nf, 1);
-        search_net(sh, g, st, a, w, t.store_path + (int64_t)nf * t.slot_cap, t.slot_cap, stats);
+        search_net<L>(sh, g, st, a, w, t.store_path + (int64_t)nf * t.slot_cap, t.slot_cap, stats);
         fin = sh.status;
         len = sh.len;
         flags |= 2;
@@ -1457,6 +1488,7 @@ pass_ripup_kernel(ogr_graph g, ogr_state st, ogr_net_table t, ogr_pass_args pa, 
 
 // After the whole-lattice search of net order[k]: the fallback ROI search if
 // it failed and the pass has fallbacks left, then the commit.
+template <int L>
 __global__ void __launch_bounds__(kThreads, 1)
 pass_full_tail_kernel(ogr_graph g, ogr_state st, ogr_net_table t, ogr_pass_args pa, int32_t k, Ws w,
                       const int32_t* full_res) {
@@ -1477,7 +1509,7 @@ pass_full_tail_kernel(ogr_graph g, ogr_state st, ogr_net_table t, ogr_pass_args 
   const int used = (int)w.result[2];
   if (fin != OGR_OK && used < pa.fallback_quota) {
     const ogr_net_args a = ogr_pass_net_args(t, pa, n, 1);
-    search_net(sh, g, st, a, w, slot, t.slot_cap, reinterpret_cast<unsigned long long*>(pa.stats));
+    search_net<L>(sh, g, st, a, w, slot, t.slot_cap, reinterpret_cast<unsigned long long*>(pa.stats));
     fin = sh.status;
     len = sh.len;
     if (fin < 0) {
@@ -1534,6 +1566,13 @@ extern "C" int ogr_window_workspace_init(void* ws, int32_t num_nodes, int32_t ma
 
 extern "C" size_t ogr_window_ctl_bytes(int32_t slots) { return win_ctl_layout(slots, nullptr, nullptr, nullptr); }
 
+extern "C" int ogr_search_lanes(int32_t lanes, int32_t* current) {
+  if (lanes != 0 && lanes != 2 && lanes != 4 && lanes != 8 && lanes != 16) return OGR_ERR_ARG;
+  if (lanes != 0) g_search_lanes = lanes;
+  if (current) *current = g_search_lanes;
+  return OGR_OK;
+}
+
 extern "C" int ogr_search_profile(int64_t* out16, int32_t reset) {
   if (!out16) return OGR_ERR_ARG;
   OGR_CUDA_TRY(cudaMemcpyFromSymbol(out16, g_stage, sizeof(unsigned long long) * 16));
@@ -1562,7 +1601,7 @@ extern "C" int ogr_find_path(const ogr_graph* g, const ogr_state* st, const ogr_
   Ws w;
   ws_layout(g->num_nodes, (char*)ws, &w);
   cudaStream_t s = ogr_stream(stream);
-  find_path_kernel<<<1, kThreads, 0, s>>>(*g, *st, *net, w, path_out, path_cap, stats);
+  OGR_WITH_LANES(L, find_path_kernel<L><<<1, kThreads, 0, s>>>(*g, *st, *net, w, path_out, path_cap, stats));
   OGR_LAUNCH_CHECK();
   int64_t res[2];
   OGR_CUDA_TRY(cudaMemcpyAsync(res, w.result, sizeof(res), cudaMemcpyDeviceToHost, s));
@@ -1592,8 +1631,8 @@ extern "C" int ogr_find_path_roi(const ogr_graph* g, const float* costs, const i
   a.full_graph = 0;
   a.penalty_enabled = 0;
   cudaStream_t s = ogr_stream(stream);
-  find_path_given_roi_kernel<<<1, kThreads, 0, s>>>(*g, st, a, w, roi_nodes, n_roi, roi_penalty, path_out, path_cap,
-                                                    stats);
+  OGR_WITH_LANES(L, find_path_given_roi_kernel<L><<<1, kThreads, 0, s>>>(*g, st, a, w, roi_nodes, n_roi, roi_penalty,
+                                                                          path_out, path_cap, stats));
   OGR_LAUNCH_CHECK();
   int64_t res[2];
   OGR_CUDA_TRY(cudaMemcpyAsync(res, w.result, sizeof(res), cudaMemcpyDeviceToHost, s));
@@ -1638,8 +1677,8 @@ extern "C" int ogr_find_path_multi(const ogr_graph* g, const float* costs, const
   a.full_graph = 0;
   a.penalty_enabled = 0;
   cudaStream_t s = ogr_stream(stream);
-  find_path_multi_kernel<<<1, kThreads, 0, s>>>(*g, st, a, w, roi_nodes, n_roi, roi_penalty, ms, path_out, path_cap,
-                                                stats);
+  OGR_WITH_LANES(L, find_path_multi_kernel<L><<<1, kThreads, 0, s>>>(*g, st, a, w, roi_nodes, n_roi, roi_penalty, ms,
+                                                                      path_out, path_cap, stats));
   OGR_LAUNCH_CHECK();
   int64_t res[2];
   OGR_CUDA_TRY(cudaMemcpyAsync(res, w.result, sizeof(res), cudaMemcpyDeviceToHost, s));
@@ -1677,7 +1716,8 @@ extern "C" int ogr_path_apply(const ogr_graph* g, const ogr_state* st, const int
 }
 
 // Window-pass grid size: one 1024-thread CTA per SM, at most `slots`.
-static int window_grid(int slots) {
+template <int L>
+static int window_grid_for(int slots) {
   static int per_dev[64] = {};
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 0;
@@ -1685,11 +1725,17 @@ static int window_grid(int slots) {
     int sms = 0, per_sm = 0, coop = 0;
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
     if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) != cudaSuccess || !coop) return 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, window_pass_kernel, kThreads, 0) != cudaSuccess)
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, window_pass_kernel<L>, kThreads, 0) != cudaSuccess)
       return 0;
     per_dev[dev] = sms * per_sm;
   }
   return slots < per_dev[dev] ? slots : per_dev[dev];
+}
+
+static int window_grid(int slots) {
+  int grid = 0;
+  OGR_WITH_LANES(L, grid = window_grid_for<L>(slots));
+  return grid;
 }
 
 extern "C" int ogr_route_pass(const ogr_graph* g, const ogr_state* st, const ogr_net_table* t,
@@ -1737,7 +1783,7 @@ extern "C" int ogr_route_pass(const ogr_graph* g, const ogr_state* st, const ogr
   // one run of ROI nets: batched windows, or the single-CTA sequential pass
   auto roi_segment = [&](const ogr_pass_args& seg) -> int {
     if (!windows) {
-      route_pass_kernel<<<1, kThreads, 0, s>>>(*g, *st, *t, seg, rbv, batch ? 1 : 0, w);
+      OGR_WITH_LANES(L, route_pass_kernel<L><<<1, kThreads, 0, s>>>(*g, *st, *t, seg, rbv, batch ? 1 : 0, w));
       OGR_LAUNCH_CHECK();
       return OGR_OK;
     }
@@ -1753,7 +1799,9 @@ extern "C" int ogr_route_pass(const ogr_graph* g, const ogr_state* st, const ogr
     char* ctl = (char*)win->ctl;
     Ws wv = w;
     void* args[] = {&gv, &sv, &tv, &pv, &rbv, &slot_base, &slot_bytes, &rmax, &scratch, &ctl, &wv};
-    OGR_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)window_pass_kernel, dim3(grid), dim3(kThreads), args, 0,
+    const void* wk = nullptr;
+    OGR_WITH_LANES(L, wk = (const void*)window_pass_kernel<L>);
+    OGR_CUDA_TRY(cudaLaunchCooperativeKernel(wk, dim3(grid), dim3(kThreads), args, 0,
                                              s));
     return OGR_OK;
   };
@@ -1778,7 +1826,7 @@ extern "C" int ogr_route_pass(const ogr_graph* g, const ogr_state* st, const ogr
         job.stats = reinterpret_cast<unsigned long long*>(pa->stats);
         const int rc = ogr_full::launch(*g, *st, job, full_ws, s);
         if (rc != OGR_OK) return rc;
-        pass_full_tail_kernel<<<1, kThreads, 0, s>>>(*g, *st, *t, *pa, k, w, full_res);
+        OGR_WITH_LANES(L, pass_full_tail_kernel<L><<<1, kThreads, 0, s>>>(*g, *st, *t, *pa, k, w, full_res));
         OGR_LAUNCH_CHECK();
         ++k;
       } else {
@@ -1850,7 +1898,7 @@ extern "C" int ogr_find_path_noalloc(const ogr_graph* g, const ogr_state* st, co
   cudaStream_t s = ogr_stream(stream);
   // The array keeps whatever the previous call left: clear seen[] / g2r[].
   ws_init_kernel<<<ogr_blocks(g->num_nodes, 256), 256, 0, s>>>(w, g->num_nodes);
-  find_path_kernel<<<1, kThreads, 0, s>>>(*g, *st, *net, w, path_out, path_cap, stats);
+  OGR_WITH_LANES(L, find_path_kernel<L><<<1, kThreads, 0, s>>>(*g, *st, *net, w, path_out, path_cap, stats));
   OGR_LAUNCH_CHECK();
   int64_t res[2];
   OGR_CUDA_TRY(cudaMemcpyAsync(res, w.result, sizeof(res), cudaMemcpyDeviceToHost, s));

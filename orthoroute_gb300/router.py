@@ -963,12 +963,14 @@ class PathFinderRouter:
         return ordered
 
     def _autotune(self, tasks):
-        """full_engine="auto": time the job's longest full-graph nets on the
-        current costs under each engine / grid and keep the fastest (the
-        choice changes no result)."""
+        """full_engine="auto": time the job's longest full-graph nets under
+        each engine / grid, and a spread of its ROI nets under each lanes per
+        node, on the current costs, and keep the fastest (the choices change
+        no result)."""
         from . import autotune
         nets = autotune.sample_full_nets(tasks, self._manhattan, ROI_THRESHOLD_STEPS)
-        self.tuning = autotune.tune(self.ops, self.lattice, nets)
+        roi_nets = autotune.sample_roi_nets(tasks, self._manhattan, ROI_THRESHOLD_STEPS)
+        self.tuning = autotune.tune(self.ops, self.lattice, nets, roi_nets)
         self.full_engine = self.tuning.full_engine
 
     def _route_all(self, tasks, all_tasks):

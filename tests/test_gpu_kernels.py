@@ -436,3 +436,50 @@ def test_autotune_times_every_candidate(tmp_path, monkeypatch):
         assert t2.cached and (t2.full_engine, t2.full_ctas) == (t.full_engine, t.full_ctas)
     finally:
         autotune.full_grid(cur)
+
+
+@pytest.mark.parametrize("lanes", [2, 8, 16])
+def test_find_path_any_lanes_per_node(lanes):
+    """The autotuner's lane widths of the ROI search: the same paths and heap
+    statistics as the oracle at 2, 8 and 16 lanes per node (4 is the default)."""
+    from orthoroute_gb300.autotune import search_lanes
+    g, s, ops, ref = make(48, 40, 6)
+    rng = np.random.default_rng(70 + lanes)
+    E, N = g.E, g.N
+    costs = (0.12 + rng.integers(0, 3, size=E) * 0.01).astype(np.float32)   # ties
+    costs[rng.choice(E, size=E // 20, replace=False)] = np.float32("inf")
+    s.total_cost.copy_(torch.from_numpy(costs))
+    net_id = 5
+    ns = _penalty_state(s, N, rng, net_id)
+    before = search_lanes(0)
+    try:
+        search_lanes(lanes)
+        for _ in range(5):
+            src, dst = (int(v) for v in rng.integers(0, ref.plane, size=2))
+            r = roi_radius(src, dst, ref.nx, ref.plane)
+            roi, g2r = extract_roi_bfs(ref.indptr, ref.indices, N, src, dst, initial_radius=r)
+            pen = ns.owner_penalty(roi, net_id, 2.3)
+            st = {}
+            want = find_path_roi(ref.indptr, ref.indices, src, dst, costs, roi, g2r, node_penalty=pen, stats=st)
+            ops.stats.zero_()
+            got = ops.find_path(ops.net_args(net_id, src, dst, max_depth=min(r, 80), halo=2, pres_fac=2.3))
+            assert got == want, (lanes, src, dst)
+            if want is not None:
+                assert ops.stats.cpu().tolist()[:2] == [st["scanned"], st["settled"]]
+    finally:
+        search_lanes(before)
+
+
+def test_autotune_picks_roi_lanes(tmp_path, monkeypatch):
+    from orthoroute_gb300 import Lattice, autotune
+    monkeypatch.setenv("ORTHOROUTE_GB300_TUNE_CACHE", str(tmp_path / "tune.json"))
+    g, s, ops, ref = make(60, 50, 6)
+    s.total_cost.copy_(torch.from_numpy(_costs(3, g.E, np.random.default_rng(2))))
+    before = autotune.search_lanes(0)
+    try:
+        roi_nets = [(3 + 61 * k, 3 + 61 * k + 20) for k in range(6)]
+        t = autotune.tune(ops, Lattice(60, 50, 6), [], roi_nets)
+        assert {f"roi_lanes{k}" for k in autotune.LANES} <= set(t.ms_per_search)
+        assert t.roi_lanes in autotune.LANES and autotune.search_lanes(0) == t.roi_lanes
+    finally:
+        autotune.search_lanes(before)

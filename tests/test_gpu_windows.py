@@ -61,10 +61,16 @@ def _run(window_slots, seed):
     return out, state
 
 
-@pytest.mark.parametrize("seed", [3, 11])
-def test_windows_match_sequential_pass(seed):
-    seq, seq_state = _run(0, seed)
-    win, win_state = _run(16, seed)
+@pytest.mark.parametrize("seed,lanes", [(3, 4), (11, 4), (3, 2)])
+def test_windows_match_sequential_pass(seed, lanes):
+    from orthoroute_gb300.autotune import search_lanes
+    before = search_lanes(0)
+    try:
+        search_lanes(lanes)
+        seq, seq_state = _run(0, seed)
+        win, win_state = _run(16, seed)
+    finally:
+        search_lanes(before)
     failed = 0
     for (s0, st0, l0, p0, a0), (s1, st1, l1, p1, a1) in zip(seq, win):
         np.testing.assert_array_equal(s0, s1)
