@@ -1606,7 +1606,8 @@ class PathFinderRouter:
                     pass
             if iteration_cb:
                 try:
-                    iteration_cb(it, [], [], over_sum, over_cnt)
+                    tracks, vias = self._paths_geometry()
+                    iteration_cb(it, tracks, vias, over_sum, over_cnt)
                 except Exception:
                     pass
             if failed == 0 and clean:
@@ -1747,15 +1748,20 @@ class PathFinderRouter:
 
 
     # ------------------------------------------------------------- geometry (F4)
-    def emit_geometry(self, board=None) -> Tuple[int, int]:
-        """``emit_geometry`` (:11316-11404) for tuple requests: tracks and vias of
-        every routed path; the export payload is kept only without overuse."""
+    def _paths_geometry(self):
+        """``_generate_geometry_from_paths`` (:11439-11563) of the current paths;
+        also what each iteration hands to ``iteration_cb`` (:7175-7227)."""
         from .geometry import GridGeometry, generate_geometry
         L = self.lattice
         axes = [L.allowed_axes(z) for z in range(L.nz)]
-        tracks, vias = generate_geometry(self.net_paths, L.nx, L.ny, L.nz, axes, GridGeometry(self.bounds, L.pitch),
-                                         self.config.layer_names, self.config.track_width, self.config.via_diameter,
-                                         self.config.via_drill)
+        return generate_geometry(self.net_paths, L.nx, L.ny, L.nz, axes, GridGeometry(self.bounds, L.pitch),
+                                 self.config.layer_names, self.config.track_width, self.config.via_diameter,
+                                 self.config.via_drill)
+
+    def emit_geometry(self, board=None) -> Tuple[int, int]:
+        """``emit_geometry`` (:11316-11404) for tuple requests: tracks and vias of
+        every routed path; the export payload is kept only without overuse."""
+        tracks, vias = self._paths_geometry()
         self._provisional_geometry = GeometryPayload(tracks, vias)
         over_sum, _ = self._compute_overuse()
         self._geometry_payload = GeometryPayload(tracks, vias) if over_sum == 0 else GeometryPayload([], [])

@@ -38,6 +38,7 @@ class RouteJob:
     bounds: Optional[Tuple[float, float, float, float]] = None
     allowed_via_spans: Optional[Sequence[Tuple[int, int]]] = None
     arrival: float = 0.0          # seconds after the server start (used by run_stream)
+    ors_path: Optional[str] = None  # when set, the job's solution is also written there as .ORS
 
 
 @dataclass
@@ -189,8 +190,11 @@ class RouteServer:
                                  window_slots=self.window_slots)
             r.initialize_lattice(Lattice(job.nx, job.ny, job.nz, allowed_via_spans=job.allowed_via_spans),
                                  job.bounds)
+            t0 = time.perf_counter()
             out = r.route_multiple_nets(list(job.requests))
             stream.synchronize()
+            if job.ors_path:
+                write_job_ors(r, out, job.name, job.ors_path, time.perf_counter() - t0)
         return {"paths": {k: list(v) for k, v in out["paths"].items()},
                 **{k: out.get(k) for k in ("success", "converged", "iterations", "overuse_sum",
                                            "barrel_conflicts", "failed_nets")}}
@@ -213,6 +217,20 @@ class RouteServer:
                 "jobs_per_s": (len(results) / span) if span > 0 else float("nan"),
                 "errors": sum(r.error is not None for r in results),
                 "peak_concurrent": self.peak_running, "peak_hbm_bytes": self.peak_bytes}
+
+
+def write_job_ors(router, result: Dict, name: str, path: str, seconds: float) -> None:
+    """The job's geometry, per-iteration metrics and outcome as a .ORS file
+    (the layout of the reference's headless export, main.py:594-662)."""
+    from .ors import export_solution_to_ors
+    router.emit_geometry()
+    metrics = [{"iteration": m.get("iter", 0), "overuse": m.get("overuse_edges", 0),
+                "nets_routed": m.get("nets_routed", 0), "overflow": m.get("overuse_sum", 0),
+                "time": m.get("iter_time_s", 0.0)} for m in result.get("iteration_metrics", [])]
+    metadata = {"total_iterations": result.get("iterations", len(metrics)), "converged": bool(result.get("converged")),
+                "total_time": seconds, "nets_routed": result.get("nets_routed", 0), "board_name": name,
+                "notes": f"barrel_conflicts={result.get('barrel_conflicts', 0)} failed_nets={result.get('failed_nets', 0)}"}
+    export_solution_to_ors(router.get_geometry_payload(), metrics, metadata, path, compress=True)
 
 
 def _num_edges(lat) -> int:

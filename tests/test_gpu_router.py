@@ -115,7 +115,11 @@ def test_gpu_router_trivial_and_skipped_requests(mode):
     skipped = [("N99", np.int64(5), 9)]
     R = gpu_router(nx, ny, nz, iters, mode)
     R.trace = []
-    res = R.route_multiple_nets(reqs + trivial + skipped)
+    seen = []
+    res = R.route_multiple_nets(reqs + trivial + skipped,
+                                iteration_cb=lambda it, tr, vi, osum, ocnt: seen.append((it, tr, vi)))
+    assert [it for it, _, _ in seen] == list(range(1, len(seen) + 1)) and len(seen) == res["iterations"]
+    assert all(t["net"] in R.net_paths for _, tr, _ in seen for t in tr) and seen[-1][1]   # provisional geometry
     assert "N99" not in R.net_paths
     assert all(R.net_paths[n] == [s] for n, s, _ in trivial)
     O = OracleRouter(LatticeSpec(nx, ny, nz), board_bounds(nx, ny), Config(max_iterations=iters), fast=True)

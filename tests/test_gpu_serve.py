@@ -43,3 +43,19 @@ def test_jobs_alone_and_in_the_mix_agree():
     for a, m in zip(alone, mixed):
         assert a.error is None and m.error is None, (a.error, m.error)
         assert a.result == m.result, a.name
+
+
+def test_job_writes_its_solution_as_ors(tmp_path):
+    from orthoroute_gb300 import ors
+    job = _jobs()[0]
+    job.ors_path = str(tmp_path / "J0.ORS")
+    srv = RouteServer(slots=1)
+    res = srv.submit(job).result()
+    srv.close()
+    assert res.error is None, res.error
+    geom, md = ors.import_solution_from_ors(job.ors_path)
+    assert md["metadata"]["board_name"] == "J0"
+    assert md["metadata"]["total_iterations"] == res.result["iterations"]
+    assert len(md["iteration_metrics"]) == res.result["iterations"]
+    routed = {n for n, p in res.result["paths"].items() if len(p) >= 2}
+    assert set(geom["by_net"]) <= routed and geom["all_tracks"]
