@@ -245,6 +245,23 @@ int ogr_find_path_multi(const ogr_graph* g, const float* costs, const int32_t* r
                         int32_t* path_out, int32_t path_cap, int32_t* path_len_out,
                         int64_t* stats, void* stream);
 
+/* Commit many paths in one launch, as the best-state restore re-commits
+ * every path (_restore_routing_state, unified_pathfinder.py:7806-7838, with
+ * commit_path :1096-1135, _rebuild_path_node_use :4623, _rebuild_node_owner
+ * :4744): present +1 on both arcs of each hop, path-node use +1, barrel
+ * ownership of every via-spanned node, no live refresh.  Path k is
+ * nodes[offsets[k] .. offsets[k+1]) (device int32, >= 2 nodes each) of net
+ * net_ids[k]; its arcs (forward then reverse) go to
+ * arcs_out[2 * (offsets[k] - k) ..].  With store_path / store_len (may be
+ * NULL) the path is also written to slot store_slot[k] of a path store with
+ * slot_cap nodes per slot.  The paths must not be committed already; the
+ * result equals committing them one by one in any order.  *status_dev:
+ * 0, 1 (a hop is not an arc) or 2 (capacity).  Asynchronous. */
+int ogr_paths_commit(const ogr_graph* g, const ogr_state* st, const int32_t* nodes, const int32_t* offsets,
+                     const int32_t* net_ids, int32_t n_paths, int32_t* arcs_out, int32_t* store_path,
+                     int32_t* store_len, const int32_t* store_slot, int32_t slot_cap,
+                     int32_t* status_dev, void* stream);
+
 /* Commit (sign=+1) or rip up (sign=-1) a path given as device node ids:
  * present +-1 (floored at 0), live-present refresh of those arcs when
  * live != 0, path-node use +-1, barrel ownership of every node spanned by a

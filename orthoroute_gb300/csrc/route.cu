@@ -1075,6 +1075,75 @@ path_apply_kernel(ogr_graph g, ogr_state st, const int32_t* path, int32_t len, i
   if (threadIdx.x == 0) *status = rc;
 }
 
+// Commit many paths at once (a best-state restore, _restore_routing_state
+// :7806-7838): present +1 on both arcs of every hop, path-node use +1, barrel
+// ownership of every via-spanned node; no live refresh.  Commits only add
+// exact small integers (and XOR ids), so paths may be applied by different
+// CTAs in any order and the state equals the sequential one.  Path k is
+// nodes[off[k] .. off[k+1]); its arcs go to arcs[2 * (off[k] - k) ..]; with a
+// store given, the path is also written to slot store_slot[k].
+__global__ void __launch_bounds__(kApplyThreads)
+paths_commit_kernel(ogr_graph g, ogr_state st, const int32_t* nodes, const int32_t* off, const int32_t* net_ids,
+                    int32_t n_paths, int32_t* arcs, int32_t* store_path, int32_t* store_len,
+                    const int32_t* store_slot, int32_t slot_cap, int32_t* status) {
+  __shared__ int32_t s_via[kMaxViaNodes];
+  __shared__ int s_nv, s_bad;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int32_t plane = g.nx * g.ny;
+  for (int32_t k = blockIdx.x; k < n_paths; k += gridDim.x) {
+    const int32_t o = off[k], len = off[k + 1] - off[k];
+    const int32_t* path = nodes + o;
+    const int hops = len - 1;
+    int32_t* a_out = arcs + 2 * (int64_t)(o - k);
+    if (tid == 0) { s_nv = 0; s_bad = 0; }
+    __syncthreads();
+    for (int i = tid; i < hops; i += nt) {
+      const int32_t u = path[i], v = path[i + 1];
+      int32_t f = -1;
+      for (int32_t e = g.indptr[u]; e < g.indptr[u + 1]; ++e)
+        if (g.indices[e] == v) { f = e; break; }
+      if (f < 0) { s_bad = 1; continue; }
+      const int32_t r = g.rev[f];
+      a_out[i] = f;
+      a_out[hops + (hops - 1 - i)] = r;
+      atomicAdd(&st.present[f], 1.0f);
+      atomicAdd(&st.present[r], 1.0f);
+    }
+    for (int i = tid; i < len; i += nt) atomicAdd(&st.path_node_use[path[i]], 1);
+    if (store_path != nullptr && len <= slot_cap)
+      for (int i = tid; i < len; i += nt) store_path[(int64_t)store_slot[k] * slot_cap + i] = path[i];
+    __syncthreads();
+    if (tid == 0) {
+      int nv = 0;
+      for (int i = 0; i < hops && !s_bad; ++i) {
+        const int32_t u = path[i], v = path[i + 1];
+        const int32_t ru = u % plane, rv = v % plane;
+        const int zu = u / plane, zv = v / plane;
+        if (ru != rv || zu == zv) continue;
+        for (int z = min(zu, zv); z <= max(zu, zv); ++z) {
+          const int32_t nd = z * plane + ru;
+          bool dup = false;
+          for (int q = 0; q < nv; ++q)
+            if (s_via[q] == nd) { dup = true; break; }
+          if (dup) continue;
+          if (nv >= kMaxViaNodes) { s_bad = 2; break; }
+          s_via[nv++] = nd;
+        }
+      }
+      s_nv = nv;
+      if (store_len != nullptr) store_len[store_slot[k]] = len <= slot_cap ? len : 0;
+      if (len > slot_cap && store_path != nullptr) s_bad = 2;
+    }
+    __syncthreads();
+    for (int q = tid; q < s_nv; q += nt) {
+      atomicAdd(&st.owner_count[s_via[q]], 1);
+      atomicXor(&st.owner_xor[s_via[q]], net_ids[k]);
+    }
+    if (tid == 0 && s_bad) atomicMax(status, s_bad);
+    __syncthreads();
+  }
+}
+
 // Extract the (cost-independent) ROIs of every ROI net of the pass, one net
 // per CTA at a time, each CTA with its own BFS slot.  roi_len[n] = -1 when a
 // queue overflowed (the pass then extracts that ROI inline).
@@ -1703,6 +1772,23 @@ extern "C" int ogr_extract_roi(const ogr_graph* g, const ogr_net_args* net, void
   OGR_CUDA_TRY(cudaStreamSynchronize(s));
   *roi_len_out = (int32_t)res[1];
   return (int)res[0];
+}
+
+extern "C" int ogr_paths_commit(const ogr_graph* g, const ogr_state* st, const int32_t* nodes, const int32_t* offsets,
+                                const int32_t* net_ids, int32_t n_paths, int32_t* arcs_out, int32_t* store_path,
+                                int32_t* store_len, const int32_t* store_slot, int32_t slot_cap, int32_t* status_dev,
+                                void* stream) {
+  if (!g || !st || n_paths < 0 || !status_dev) return OGR_ERR_ARG;
+  if (n_paths == 0) return OGR_OK;
+  if (!nodes || !offsets || !net_ids || !arcs_out || ((store_path || store_len) && (!store_slot || slot_cap < 2)))
+    return OGR_ERR_ARG;
+  cudaStream_t s = ogr_stream(stream);
+  OGR_CUDA_TRY(cudaMemsetAsync(status_dev, 0, sizeof(int32_t), s));
+  const int grid = n_paths < 152 * 8 ? n_paths : 152 * 8;
+  paths_commit_kernel<<<grid, kApplyThreads, 0, s>>>(*g, *st, nodes, offsets, net_ids, n_paths, arcs_out, store_path,
+                                                      store_len, store_slot, slot_cap, status_dev);
+  OGR_LAUNCH_CHECK();
+  return OGR_OK;
 }
 
 extern "C" int ogr_path_apply(const ogr_graph* g, const ogr_state* st, const int32_t* path, int32_t len,

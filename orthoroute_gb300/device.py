@@ -322,6 +322,43 @@ class Ops:
                                             self.g.N, C.byref(n), self._sp()), "ogr_extract_roi")
         return out[: n.value].cpu().numpy()
 
+    def commit_paths(self, paths: Sequence[np.ndarray], net_ids: Sequence[int], store: "PathStore" = None,
+                     slots: Optional[Sequence[int]] = None) -> List[np.ndarray]:
+        """Commit many paths (>= 2 nodes each) in one launch, no live refresh
+        (a best-state restore); optionally into `store` slots.  Returns each
+        path's arcs (forward then reverse) as int64 arrays."""
+        n = len(paths)
+        if n == 0:
+            return []
+        lens = np.fromiter((len(p) for p in paths), dtype=np.int64, count=n)
+        if lens.min() < 2:
+            raise ValueError("commit_paths takes paths of two or more nodes")
+        off = np.zeros(n + 1, dtype=np.int32)
+        off[1:] = np.cumsum(lens)
+        flat = np.concatenate([np.asarray(p, dtype=np.int32) for p in paths])
+        dev = self.g.device
+        d_nodes = torch.from_numpy(flat).to(dev)
+        d_off = torch.from_numpy(off).to(dev)
+        d_ids = torch.from_numpy(np.asarray(net_ids, dtype=np.int32)).to(dev)
+        arcs = torch.empty(int(2 * (lens - 1).sum()), dtype=torch.int32, device=dev)
+        d_slots = None if store is None else torch.from_numpy(np.asarray(slots, dtype=np.int32)).to(dev)
+        g = self.g.cgraph()
+        st = self.s.cstate()
+        _lib.check(self.lib.ogr_paths_commit(C.byref(g), C.byref(st), _p(d_nodes), _p(d_off), _p(d_ids), n, _p(arcs),
+                                             _p(store.path) if store is not None else None,
+                                             _p(store.length) if store is not None else None, _p(d_slots),
+                                             store.slot_cap if store is not None else 0, _p(self.status),
+                                             self._sp()), "ogr_paths_commit")
+        a = arcs.cpu().numpy().astype(np.int64)
+        self.counters["launches"] += 1
+        self.counters["h2d_bytes"] += flat.nbytes + off.nbytes + 4 * n * (2 if store is not None else 1)
+        self.counters["d2h_bytes"] += 4 * a.size + 4
+        bad = int(self.status.item())
+        if bad:
+            raise ValueError("path hop is not a graph edge" if bad == 1 else "path longer than the path-store slot")
+        aoff = 2 * (off[:-1].astype(np.int64) - np.arange(n))
+        return [a[aoff[k]: aoff[k] + 2 * (lens[k] - 1)] for k in range(n)]
+
     def apply_path(self, path: Sequence[int], net_id: int, sign: int, pres_fac: float, live: bool = True):
         """Commit (+1) or rip up (-1); returns the arc list (forward then reverse)."""
         L = len(path)

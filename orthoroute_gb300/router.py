@@ -747,18 +747,38 @@ class PathFinderRouter:
     def _edge_over(self, over_idx, over_val):
         """For every tracked net: (Σ over values of its arcs in its arc order —
         the left-to-right float sum of the reference's generator — and whether
-        any of its arcs is in over_idx).  over_idx: sorted arc ids."""
+        any of its arcs is in over_idx).  over_idx: sorted arc ids.  The
+        overused arcs are looked up through a dense arc-indexed scratch array;
+        the result is reused while neither the tracking nor the overuse
+        changed (the hotset and the net order of one iteration ask the same)."""
         names, flat, owner = self._edge_index()
         k = len(names)
-        if k == 0 or len(over_idx) == 0:
-            return names, np.zeros(k, dtype=np.float64), np.zeros(k, dtype=bool)
         oi = np.asarray(over_idx, dtype=np.int64)
-        pos = np.minimum(np.searchsorted(oi, flat), oi.size - 1)
-        hit = oi[pos] == flat
-        w = np.where(hit, np.asarray(over_val, dtype=np.float64)[pos], 0.0)
-        sums = np.bincount(owner, weights=w, minlength=k)
-        anyhit = np.bincount(owner, weights=hit.astype(np.float64), minlength=k) > 0
-        return names, sums, anyhit
+        ov = np.asarray(over_val, dtype=np.float64)
+        c = getattr(self, "_edge_over_cache", None)
+        if c is not None and c[0] is self._eidx and np.array_equal(c[1], oi) and np.array_equal(c[2], ov):
+            return c[3]
+        if k == 0 or oi.size == 0:
+            out = (names, np.zeros(k, dtype=np.float64), np.zeros(k, dtype=bool))
+        else:
+            dense = getattr(self, "_over_dense", None)
+            if dense is None or dense.size != self.E:
+                dense = self._over_dense = np.zeros(self.E, dtype=np.float64)
+                self._over_mask = np.zeros(self.E, dtype=bool)
+            mask = self._over_mask
+            dense[oi] = ov
+            mask[oi] = True
+            try:
+                hit = mask[flat]
+                w = dense[flat]
+            finally:
+                dense[oi] = 0.0
+                mask[oi] = False
+            sums = np.bincount(owner, weights=w, minlength=k)
+            anyhit = np.bincount(owner, weights=hit.astype(np.float64), minlength=k) > 0
+            out = (names, sums, anyhit)
+        self._edge_over_cache = (self._eidx, oi.copy(), ov.copy(), out)
+        return out
 
     # ------------------------------------------------------------- tallies
     def _compute_overuse(self):
@@ -1269,10 +1289,14 @@ class PathFinderRouter:
         self._eidx = None
         if self.store is not None:
             self.store.length.zero_()
-        for n, p in self.net_paths.items():
-            if not p or len(p) < 2:
-                continue
-            edges = self._apply(n, p, +1, live=False)
+        # every path committed in one launch (commits add exact counts, so the
+        # state equals the reference's path-by-path re-commit)
+        names = [n for n, p in self.net_paths.items() if p and len(p) >= 2]
+        arrs = [self._net_paths.array(n) for n in names]
+        ids = [self._net_id(n) for n in names]
+        slots = [self._task_index[n] for n in names] if self.store is not None else None
+        for n, a, edges in zip(names, arrs, self.ops.commit_paths(arrs, ids, self.store, slots)):
+            self._mark_nodes(n, None, +1, a)
             self._update_tracking(n, edges)
         self._add_trivial_use()
         self._rebuild_via_usage()

@@ -483,3 +483,42 @@ def test_autotune_picks_roi_lanes(tmp_path, monkeypatch):
         assert t.roi_lanes in autotune.LANES and autotune.search_lanes(0) == t.roi_lanes
     finally:
         autotune.search_lanes(before)
+
+
+def test_commit_paths_equals_one_by_one():
+    """The batched restore commit: the same present, path-node use, barrel
+    ownership, arcs and path-store slots as committing the paths one at a time."""
+    from orthoroute_gb300.device import PathStore
+    rng = np.random.default_rng(12)
+    nx, ny, nz = 30, 24, 8
+    paths = []                   # simple random walks over the lattice's arcs
+    g, s, ops, ref = make(nx, ny, nz)
+    indptr, indices = ref.indptr, ref.indices
+    for k in range(60):
+        node = int(rng.integers(0, ref.num_nodes))
+        p, seen = [node], {node}
+        for _ in range(int(rng.integers(1, 40))):
+            nb = [int(v) for v in indices[indptr[p[-1]]:indptr[p[-1] + 1]] if int(v) not in seen]
+            if not nb:
+                break
+            p.append(nb[int(rng.integers(0, len(nb)))])
+            seen.add(p[-1])
+        if len(p) >= 2:
+            paths.append(p)
+    ids = [3 + k for k in range(len(paths))]
+    # one by one
+    one = [ops.apply_path(p, i, +1, 1.0, live=False) for p, i in zip(paths, ids)]
+    want = {k: getattr(s, k).cpu().numpy().copy() for k in ("present", "path_node_use", "owner_count", "owner_xor")}
+    for k in want:
+        getattr(s, k).zero_()
+    store = PathStore(g, len(paths) + 5)
+    slots = [len(paths) + 4 - k for k in range(len(paths))]
+    got_arcs = ops.commit_paths([np.asarray(p) for p in paths], ids, store, slots)
+    for k, v in want.items():
+        np.testing.assert_array_equal(getattr(s, k).cpu().numpy(), v, err_msg=k)
+    for a, b in zip(got_arcs, one):
+        assert a.tolist() == list(b)
+    L = store.length.cpu().numpy()
+    P = store.path.cpu().numpy()
+    for p, sl in zip(paths, slots):
+        assert L[sl] == len(p) and P[sl, :len(p)].tolist() == p

@@ -243,6 +243,7 @@ def test_via_nodes_match_hop_loop():
 def test_edge_over_sums_match_generator_sums():
     rng = np.random.default_rng(3)
     h = _host()
+    h.E = 500
     h._eidx = None
     h.net_to_edges = {f"N{i}": rng.integers(0, 500, size=int(rng.integers(0, 40))).astype(np.int64)
                       for i in range(30)}
@@ -251,6 +252,9 @@ def test_edge_over_sums_match_generator_sums():
     over_val = (rng.random(over_idx.size).astype(np.float32) * 3).astype(np.float64)
     over_map = dict(zip(over_idx.tolist(), over_val.tolist()))
     names, sums, hit = R.PathFinderRouter._edge_over(h, over_idx, over_val)
+    again = R.PathFinderRouter._edge_over(h, over_idx, over_val)
+    assert again[0] is names and again[1] is sums                          # reused while nothing changed
+    assert not h._over_mask.any() and not h._over_dense.any()              # scratch left clean
     for i, n in enumerate(names):
         edges = h.net_to_edges[n].tolist()
         assert sums[i] == sum(float(over_map[e]) for e in edges if e in over_map)
