@@ -46,6 +46,12 @@ CONFIGS = {
     # pins inside a seeded 50x50 box per net, as star two-pin requests p0 -> pi (multipin.py)
     "c2": dict(nx=600, ny=400, nz=12, nets=1500, iters=40, seed=2468, multipin=True, via_span=4,
                plain_iters=1, plain_nets=300, searches_per_job=52476),
+    # BASELINE configs[3]: 1000x800x32 (25.6 M nodes; 32 layers allow adjacent vias only), a 40x40
+    # BGA at 1 mm (2.5 cells) in the centre and four edge-connector rows; reconciled to 1,600 BGA
+    # escape nets (ball -> seeded-random connector pin) + 3,200 backplane nets pairing the other
+    # 6,400 connector pins, every pin used once (bga_requests); iterations capped for a run
+    "c3": dict(nx=1000, ny=800, nz=32, nets=4800, iters=2, seed=1357, bga=True,
+               plain_iters=None, searches_per_job=None),
 }
 
 
@@ -97,6 +103,8 @@ def make_requests(cfg):
     if cfg.get("multipin"):
         from orthoroute_gb300.multipin import seeded_multipin_nets, star_requests
         return star_requests(seeded_multipin_nets(nx, ny, n, cfg["seed"]))
+    if cfg.get("bga"):
+        return bga_requests(nx, ny, cfg["seed"])
     rng = np.random.default_rng(cfg["seed"])
     out = []
     if not cfg["clusters"]:
@@ -119,6 +127,40 @@ def make_requests(cfg):
         if (x0, y0) == (x1, y1):
             continue
         out.append((f"N{len(out)}", y0 * nx + x0, y1 * nx + x1))
+    return out
+
+
+def connector_pins(nx, ny, per_row=2000):
+    """Four edge-connector rows of per_row pins on layer 0: the top and bottom
+    rows fill two cell rows along their edge, the left and right rows three
+    cell columns (evenly spread)."""
+    rows = []
+    for y0 in (0, ny - 2):                       # top / bottom: 2 x nx cells
+        cells = [(x, y0 + d) for x in range(nx) for d in range(2)]
+        rows.append(cells)
+    for x0 in (0, nx - 3):                       # left / right: 3 x ny cells
+        cells = [(x0 + d, y) for y in range(2, ny - 2) for d in range(3)]
+        rows.append(cells)
+    pins = []
+    for cells in rows:
+        idx = np.linspace(0, len(cells) - 1, per_row).round().astype(int)
+        pins.extend(cells[i] for i in idx)
+    return [y * nx + x for x, y in pins]
+
+
+def bga_requests(nx, ny, seed, balls=40, pitch_cells=2.5):
+    """c3's nets (see CONFIGS): BGA escapes then backplane pairs, seeded."""
+    rng = np.random.default_rng(seed)
+    cx, cy = nx / 2.0, ny / 2.0
+    off = (balls - 1) / 2.0
+    bga = [int(round(cy + (j - off) * pitch_cells)) * nx + int(round(cx + (i - off) * pitch_cells))
+           for j in range(balls) for i in range(balls)]
+    conn = connector_pins(nx, ny)
+    perm = rng.permutation(len(conn))
+    out = [(f"B{k}", bga[k], conn[perm[k]]) for k in range(len(bga))]
+    rest = perm[len(bga):]
+    for k in range(len(rest) // 2):
+        out.append((f"P{k}", conn[rest[2 * k]], conn[rest[2 * k + 1]]))
     return out
 
 
@@ -323,7 +365,9 @@ def run_ours(args, cfg, rank, world):
         "mode": args.mode,
         "full_engine": {"requested": args.full_engine, "used": router.full_engine,
                         "tuning": (None if router.tuning is None else
-                                   {"ctas": router.tuning.full_ctas, "roi_lanes": router.tuning.roi_lanes,
+                                   {"ctas": router.tuning.full_ctas, "full_lanes": router.tuning.full_lanes,
+                                    "full_reuse": router.tuning.full_reuse,
+                                    "roi_lanes": router.tuning.roi_lanes,
                                     "ms_per_search": router.tuning.ms_per_search,
                                     "cached": router.tuning.cached})},
     }

@@ -381,7 +381,7 @@ int ogr_route_pass(const ogr_graph* g, const ogr_state* st, const ogr_net_table*
  * 8219-8262, into find_path_roi :2451-2548 with roi_nodes = all nodes).  Same
  * result, statistics and status codes as ogr_find_path with
  * net->full_graph = 1, computed by one cooperative launch on all SMs.  The
- * workspace (about 36 bytes per node + 4 per arc) is initialised once with
+ * workspace (about 44 bytes per node + 4 per arc) is initialised once with
  * ogr_full_workspace_init; a search rewrites the 8-byte key word of every
  * node and otherwise touches only the nodes it reaches.
  * OGR_ERR_TIMEOUT: a grid barrier gave up (not expected; the launch is
@@ -400,6 +400,19 @@ int ogr_find_path_full(const ogr_graph* g, const ogr_state* st, const ogr_net_ar
  * setting is per device and process-wide.  Chosen by the autotuner
  * (orthoroute_gb300/autotune.py); no reference counterpart. */
 int ogr_full_grid(int32_t ctas, int32_t* current, int32_t* limit);
+
+/* Lanes per examined frontier node of the whole-lattice search (4, 8 or 16;
+ * default 16) for searches launched afterwards; 0 only reads.  A tuning
+ * knob (results do not depend on it), process-wide, chosen by the
+ * autotuner; no reference counterpart. */
+int ogr_full_lanes(int32_t lanes, int32_t* current);
+
+/* Whether the whole-lattice search keeps the last pull of a carried frontier
+ * node none of whose in-neighbours settled since (mode 1) or pulls every
+ * frontier node every phase (0, default); -1 only reads.  A tuning knob
+ * (results do not depend on it), process-wide, chosen by the autotuner; no
+ * reference counterpart. */
+int ogr_full_reuse(int32_t mode, int32_t* current);
 
 /* Lanes per node of the single-CTA ROI search (2, 4, 8 or 16; default 4) for
  * every search launched afterwards; 0 only reads.  *current (host, may be

@@ -10,8 +10,11 @@ width to tune: each phase's threshold is the least tentative label, and the
 settle rule is fixed by exactness.  So the tuner sweeps
 
 * the engine: "grid" or "cta";
-* the grid of the "grid" engine: 1/4, 1/2, 3/4 and all of the resident CTAs
-  (SMs x CTAs per SM);
+* the lanes per examined frontier node of the "grid" engine (4, 8, 16) and
+  whether waiting frontier nodes keep their last pull (on / off), timed on
+  the full grid;
+* then the grid of the "grid" engine: 1/4, 1/2, 3/4 and all of the resident
+  CTAs (SMs x CTAs per SM);
 
 on a few full-graph searches of the job's own long nets over the current
 costs, and keeps the fastest.  For ROI nets (one 1024-thread CTA per search)
@@ -42,6 +45,8 @@ class Tuning:
     full_ctas: int
     ms_per_search: Dict[str, float] = field(default_factory=dict)
     roi_lanes: int = 4
+    full_lanes: int = 16
+    full_reuse: int = 0
     samples: int = 0
     cached: bool = False
 
@@ -61,6 +66,21 @@ def search_lanes(lanes: int = 0) -> int:
 
 
 LANES = (2, 4, 8, 16)
+FULL_LANES = (4, 8, 16)
+
+
+def full_lanes(lanes: int = 0) -> int:
+    """Set (lanes > 0) or read the whole-lattice search's lanes per frontier node."""
+    cur = C.c_int32(0)
+    _lib.check(_lib.load().ogr_full_lanes(int(lanes), C.byref(cur)), "ogr_full_lanes")
+    return int(cur.value)
+
+
+def full_reuse(mode: int = -1) -> int:
+    """Set (0 / 1) or read (-1) the whole-lattice search's reuse of clean pulls."""
+    cur = C.c_int32(0)
+    _lib.check(_lib.load().ogr_full_reuse(int(mode), C.byref(cur)), "ogr_full_reuse")
+    return int(cur.value)
 
 
 def cache_path() -> str:
@@ -123,6 +143,8 @@ def tune(ops, lattice, nets: Sequence[Tuple[int, int]], roi_nets: Sequence[Tuple
             t = Tuning(**{**hit, "cached": True})
             if t.full_engine == "grid":
                 full_grid(t.full_ctas)
+                full_lanes(t.full_lanes)
+                full_reuse(t.full_reuse)
             search_lanes(t.roi_lanes)
             return t
     cur, limit = full_grid(0)
@@ -148,20 +170,34 @@ def tune(ops, lattice, nets: Sequence[Tuple[int, int]], roi_nets: Sequence[Tuple
     # one untimed search first: workspace, lazy module load and caches
     s0, d0 = nets[0]
     ops.find_path(ops.net_args(0, s0, d0, full_graph=True, penalty=False), engine="grid")
+
+    def time_full(engine):
+        ms = 0.0
+        for _ in range(repeats):
+            for s, d in nets:
+                t0 = ops.counters["search_ms"]
+                ops.find_path(ops.net_args(0, s, d, full_graph=True, penalty=False), engine=engine)
+                ms += ops.counters["search_ms"] - t0
+        return ms / max(1, repeats * len(nets))
+
+    lanes_ms = {}
+    full_grid(limit)
+    for lanes in FULL_LANES:
+        for reuse in (0, 1):
+            full_lanes(lanes)
+            full_reuse(reuse)
+            lanes_ms[(lanes, reuse)] = time_full("grid")
+            timings[f"full_lanes{lanes}_reuse{reuse}"] = round(lanes_ms[(lanes, reuse)], 4)
+    best_full_lanes, best_reuse = min(lanes_ms, key=lambda k: (lanes_ms[k], -k[0], k[1]))
+    full_lanes(best_full_lanes)
+    full_reuse(best_reuse)
     try:
         for engine, ctas in candidates(limit):
             if engine == "cta" and ops.g.N > cta_max_nodes:
                 continue        # one CTA over a lattice this large is never the faster engine
             if engine == "grid":
                 full_grid(ctas)
-            ms = 0.0
-            for _ in range(repeats):
-                for s, d in nets:
-                    net = ops.net_args(0, s, d, full_graph=True, penalty=False)
-                    t0 = ops.counters["search_ms"]
-                    ops.find_path(net, engine=engine)
-                    ms += ops.counters["search_ms"] - t0
-            ms /= max(1, repeats * len(nets))
+            ms = lanes_ms[(best_full_lanes, best_reuse)] if (engine == "grid" and ctas == limit) else time_full(engine)
             name = f"grid{ctas}" if engine == "grid" else "cta"
             timings[name] = round(ms, 4)
             if ms < best[2]:
@@ -171,7 +207,8 @@ def tune(ops, lattice, nets: Sequence[Tuple[int, int]], roi_nets: Sequence[Tuple
     engine, ctas, _ = best
     full_grid(ctas if engine == "grid" else cur)
     t = Tuning(key=key, full_engine=engine, full_ctas=ctas if engine == "grid" else cur, ms_per_search=timings,
-               samples=len(nets) + len(roi_nets), roi_lanes=best_lanes)
+               samples=len(nets) + len(roi_nets), roi_lanes=best_lanes, full_lanes=best_full_lanes,
+               full_reuse=best_reuse)
     if use_cache:
         _store_cache(path, key, t)
     return t

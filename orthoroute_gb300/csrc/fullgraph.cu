@@ -35,10 +35,17 @@ namespace cg = cooperative_groups;
 namespace {
 
 constexpr int kThreads = 512;
-constexpr int kSub = 16;                   // lanes per examined node
-constexpr int kGroups = kThreads / kSub;   // groups per CTA
+// Lanes per examined frontier node: 4, 8 or 16 (one instantiation each,
+// chosen at launch by ogr_full_lanes; results do not depend on it).  Narrow
+// groups keep more nodes in flight when rows are short and fronts are wide.
+int g_full_lanes = 16;
+// Reuse of clean carried nodes' last pull (ogr_full_reuse): it saves the
+// pulls of wide fronts of waiting nodes and costs a stamp load per entry and
+// state stores per carried node; which wins depends on the lattice.
+int g_full_reuse = 0;
 constexpr int kStage = 2048;               // staged list entries per CTA and list
 constexpr unsigned kBarSpin = 1u << 22;
+
 
 struct FCtl {
   alignas(128) unsigned long long bar_count;   // monotone arrival counter
@@ -66,7 +73,10 @@ using FEntry = int4;
 
 struct FWs {
   NodeRec* rec;
-  int32_t* par;              // winning in-neighbour, valid once settled
+  int32_t* par;              // winning in-neighbour (tentative while carried, final once settled)
+  int32_t* dirty;            // phase in which the node must pull again (an in-neighbour settled)
+  float* tcin;               // cin of a carried node's last pull
+  int32_t reuse;             // 1: carried nodes with no newly settled in-neighbour skip the pull
   float* rcost;              // reverse-arc cost gather when the state carries none
   FEntry* fr[3];             // frontier lists: read, write, and the one being cleared
   int32_t* log;              // settled nodes in settle order
@@ -87,6 +97,8 @@ size_t fws_layout(int32_t N, int64_t E, char* base, FWs* w) {
   t.ctl = (FCtl*)take(sizeof(FCtl));
   t.rec = (NodeRec*)take(16 * n);
   t.par = (int32_t*)take(4 * n);
+  t.dirty = (int32_t*)take(4 * n);
+  t.tcin = (float*)take(4 * n);
   t.rcost = (float*)take(4 * (size_t)E);
   for (int i = 0; i < 3; ++i) t.fr[i] = (FEntry*)take(16 * n);
   t.log = (int32_t*)take(4 * n);
@@ -221,8 +233,11 @@ __device__ __forceinline__ NodeRec ld_rec(const NodeRec* p) {
   return r;
 }
 
+template <int S>
 __global__ void __launch_bounds__(kThreads, 2)
 full_sssp_kernel(ogr_graph g, ogr_state st, ogr_full::Job job, FWs w) {
+  constexpr int kSub = S;                    // lanes per examined node
+  constexpr int kGroups = kThreads / kSub;   // groups per CTA
   __shared__ Smem sm;
   const int tid = threadIdx.x;
   const int lane = tid & 31;
@@ -276,11 +291,13 @@ full_sssp_kernel(ogr_graph g, ogr_state st, ogr_full::Job job, FWs w) {
   int32_t gbase = __ldcg(&ctl->gbase);
   const int max_phase = 2 * N + 4;
   if (gbase < 1 || gbase > 0x7fffffff - (max_phase + 8)) {
-    for (int64_t r = gtid; r < N; r += gthreads)
+    for (int64_t r = gtid; r < N; r += gthreads) {
+      w.dirty[r] = 0;
       if (r != src) {
         rec[r].sp = 0;
         rec[r].reach = 0;
       }
+    }
     gbase = 1;
   }
   const float* rc = st.rcost;
@@ -340,7 +357,13 @@ full_sssp_kernel(ogr_graph g, ogr_state st, ogr_full::Job job, FWs w) {
       const float pv = __int_as_float(ent.w);
       const double pd = (double)pv;
       const bool is_src = v == src;
-      const bool one_pass = f1 - f0 <= kSub;
+      // A carried node none of whose in-neighbours settled since its last
+      // pull keeps that pull's state (label in rec, parent, cin): a pull is a
+      // function of the in-neighbours settled before the phase.  A settle in
+      // phase q writes dirty = q + 1 (values only grow; a settle of this very
+      // phase may already show as gp + 1, which only adds a harmless pull).
+      const bool pull = !w.reuse || is_src || __ldcg(&w.dirty[v]) >= gp;
+      const bool one_pass = pull && f1 - f0 <= kSub;
       // pull: the lexicographic minimum of the candidates of the in-neighbours
       // settled before this phase; cin from the others.  One-pass rows keep
       // each lane's neighbour data (stamps, penalty, CSR row) for the marking.
@@ -349,7 +372,7 @@ full_sssp_kernel(ogr_graph g, ogr_state st, ogr_full::Job job, FWs w) {
       int32_t bu = 0x7fffffff;
       int32_t u0 = -1, s0 = 0, r0 = 0, i0 = 0, i1 = 0;
       float cout0 = kInf, p0 = 0.0f;
-      for (int32_t f = f0 + sl; f < f1; f += kSub) {
+      for (int32_t f = f0 + sl; pull && f < f1; f += kSub) {
         const int32_t u = indices[f];
         const float c = rc[f];
         const NodeRec ru = ld_rec(&rec[u]);
@@ -379,13 +402,29 @@ full_sssp_kernel(ogr_graph g, ogr_state st, ogr_full::Job job, FWs w) {
         if (ogr_key_lt(oa, ol, ou, ba, bl, bu)) { ba = oa; bl = ol; bu = ou; bc = oc; }
         cin = fminf(cin, tile.shfl_xor(cin, o));
       }
-      const double lv = is_src ? 0.0 : (bl + (double)bc) + pd;
-      const float m32 = is_src ? 0.0f : ba;
+      double lv;
+      float m32;
+      if (pull) {
+        lv = is_src ? 0.0 : (bl + (double)bc) + pd;
+        m32 = is_src ? 0.0f : ba;   // == float32(lv): the same expression
+      } else {
+        lv = __ldcg(&rec[v].lab);
+        m32 = __double2float_rn(lv);
+        cin = __ldcg(&w.tcin[v]);
+        bu = __ldcg(&w.par[v]);
+      }
       const bool settle = (lv == T) || m32 < __double2float_rn((T + (double)cin) + pd);
       examined += (sl == 0);
       if (!settle) {
         stage_push_tile(tile, sm, 0, sl == 0, ent, frn, &ctl->nfront[bn]);
-        if (sl == 0) atomicMin(&sm.tmin, ogr_dbits(lv));
+        if (sl == 0) {
+          atomicMin(&sm.tmin, ogr_dbits(lv));
+          if (pull && w.reuse) {   // keep the pulled state; rec[v].lab is read by others only once settled
+            rec[v].lab = lv;
+            w.tcin[v] = cin;
+            w.par[v] = bu;
+          }
+        }
         continue;
       }
       if (sl == 0) {
@@ -406,6 +445,7 @@ full_sssp_kernel(ogr_graph g, ogr_state st, ogr_full::Job job, FWs w) {
         }
         bool fresh = false;
         FEntry ny = make_int4(0, 0, 0, 0);
+        if (w.reuse && act && !(sy > gbase)) w.dirty[y] = gp + 1;   // v settled: y pulls next phase
         if (act && !(sy > gbase)) {   // settled nodes cannot improve
           const float c = one_pass ? cout0 : fcost[f];
           const float py = one_pass ? p0 : ogr_node_penalty(st, a, y);
@@ -530,7 +570,12 @@ int size_grid(int dev) {
     int sms = 0, per_sm = 0, coop = 0;
     OGR_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     OGR_CUDA_TRY(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
-    OGR_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, full_sssp_kernel, kThreads, 0));
+    // every lane width must fit the same cooperative grid
+    int p4 = 0, p8 = 0, p16 = 0;
+    OGR_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&p4, full_sssp_kernel<4>, kThreads, 0));
+    OGR_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&p8, full_sssp_kernel<8>, kThreads, 0));
+    OGR_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&p16, full_sssp_kernel<16>, kThreads, 0));
+    per_sm = min(p4, min(p8, p16));
     if (!coop || per_sm < 1) return OGR_ERR_CUDA;
     g_grid_limit[dev] = sms * per_sm;
   }
@@ -560,18 +605,35 @@ int launch(const ogr_graph& g, const ogr_state& st, const Job& job, void* ws, cu
   if (rc != OGR_OK) return rc;
   FWs w;
   fws_layout(g.num_nodes, g.num_edges, (char*)ws, &w);
+  w.reuse = g_full_reuse;
   // bar_count, bar_gen and bar_err start at zero on every launch
   OGR_CUDA_TRY(cudaMemsetAsync(w.ctl, 0, offsetof(FCtl, tbits), s));
   ogr_graph gv = g;
   ogr_state sv = st;
   ogr_full::Job jv = job;
   void* args[] = {&gv, &sv, &jv, &w};
-  OGR_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)full_sssp_kernel, dim3(g_grid_blocks[dev]), dim3(kThreads),
-                                           args, 0, s));
+  const void* fn = g_full_lanes == 4   ? (const void*)full_sssp_kernel<4>
+                   : g_full_lanes == 8 ? (const void*)full_sssp_kernel<8>
+                                       : (const void*)full_sssp_kernel<16>;
+  OGR_CUDA_TRY(cudaLaunchCooperativeKernel(fn, dim3(g_grid_blocks[dev]), dim3(kThreads), args, 0, s));
   return OGR_OK;
 }
 
 }  // namespace ogr_full
+
+extern "C" int ogr_full_lanes(int32_t lanes, int32_t* current) {
+  if (lanes != 0 && lanes != 4 && lanes != 8 && lanes != 16) return OGR_ERR_ARG;
+  if (lanes != 0) g_full_lanes = lanes;
+  if (current) *current = g_full_lanes;
+  return OGR_OK;
+}
+
+extern "C" int ogr_full_reuse(int32_t mode, int32_t* current) {
+  if (mode < -1 || mode > 1) return OGR_ERR_ARG;
+  if (mode >= 0) g_full_reuse = mode;
+  if (current) *current = g_full_reuse;
+  return OGR_OK;
+}
 
 extern "C" int ogr_full_grid(int32_t ctas, int32_t* current, int32_t* limit) {
   int dev = 0;

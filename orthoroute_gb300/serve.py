@@ -64,7 +64,7 @@ def job_footprint(nx: int, ny: int, nz: int, num_edges: int, num_nets: int, wind
     csr = 4 * (N + 1) + E * (4 + 4 + 1 + 1 + 4 + 4)
     state = E * 4 * 7 + N * 4 * 4 + 4 * nz
     roi_ws = 72 * N + 2 * 4 * min(N, 65536) * 32 + 4 * min(N, 65536)
-    full_ws = 36 * N + 4 * E
+    full_ws = 44 * N + 4 * E
     qcap = min(N, max(4 * max_roi_nodes, 1 << 18))
     bfs = min(bfs_slots, max(1, num_nets)) * (4 * N + 4 * 4 * qcap)
     window = window_slots * (4 * N + 48 * R + 8 * min(R, 65536) * 32 + slot_cap * 4)

@@ -428,7 +428,9 @@ def test_autotune_times_every_candidate(tmp_path, monkeypatch):
     try:
         t = autotune.tune(ops, lat, nets)
         assert not t.cached and t.samples == 2
-        assert set(t.ms_per_search) == {f"grid{c}" for _, c in autotune.candidates(lim)[:-1]} | {"cta"}
+        assert set(t.ms_per_search) == ({f"grid{c}" for _, c in autotune.candidates(lim)[:-1]} | {"cta"} |
+                                        {f"full_lanes{k}_reuse{r}" for k in autotune.FULL_LANES for r in (0, 1)})
+        assert autotune.full_lanes(0) == t.full_lanes and autotune.full_reuse() == t.full_reuse
         assert t.full_engine in ("grid", "cta")
         if t.full_engine == "grid":
             assert autotune.full_grid(0)[0] == t.full_ctas
@@ -436,6 +438,8 @@ def test_autotune_times_every_candidate(tmp_path, monkeypatch):
         assert t2.cached and (t2.full_engine, t2.full_ctas) == (t.full_engine, t.full_ctas)
     finally:
         autotune.full_grid(cur)
+        autotune.full_lanes(16)
+        autotune.full_reuse(0)
 
 
 @pytest.mark.parametrize("lanes", [2, 8, 16])
@@ -522,3 +526,35 @@ def test_commit_paths_equals_one_by_one():
     P = store.path.cpu().numpy()
     for p, sl in zip(paths, slots):
         assert L[sl] == len(p) and P[sl, :len(p)].tolist() == p
+
+
+@pytest.mark.parametrize("lanes,reuse", [(4, 0), (8, 0), (4, 1), (16, 1)])
+def test_full_grid_search_any_lanes(lanes, reuse):
+    """The whole-lattice search with 4, 8 or 16 lanes per frontier node, with
+    and without the reuse of clean pulls: the same paths and heap statistics
+    as the oracle (16 lanes without reuse is the default)."""
+    from orthoroute_gb300.autotune import full_lanes, full_reuse
+    g, s, ops, ref = make(120, 90, 8)
+    rng = np.random.default_rng(600 + lanes)
+    costs = _costs(lanes % 4, g.E, rng)
+    s.total_cost.copy_(torch.from_numpy(costs))
+    ident = np.arange(g.N, dtype=np.int32)
+    net_id = 2
+    ns = _penalty_state(s, g.N, rng, net_id)
+    pen = ns.owner_penalty(ident, net_id, 2.3)
+    before = full_lanes(0)
+    try:
+        full_lanes(lanes)
+        full_reuse(reuse)
+        for _ in range(3):
+            src, dst = (int(v) for v in rng.integers(0, ref.plane, size=2))
+            st = {}
+            want = find_path_roi_c(ref.indptr, ref.indices, src, dst, costs, ident, ident, node_penalty=pen, stats=st)
+            ops.stats.zero_()
+            got = ops.find_path(ops.net_args(net_id, src, dst, full_graph=True, pres_fac=2.3), engine="grid")
+            assert got == want
+            if want is not None:
+                assert ops.stats.cpu().tolist()[:2] == [st["scanned"], st["settled"]]
+    finally:
+        full_lanes(before)
+        full_reuse(0)
