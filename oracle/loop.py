@@ -24,9 +24,7 @@ streams coincide.  Every array operation keeps the reference's numpy dtypes.
 """
 from __future__ import annotations
 
-import copy
 import heapq
-import math
 import os
 import random
 from collections import defaultdict

@@ -12,7 +12,6 @@ The device builds the CSR from the per-layer partner table produced here.
 """
 from __future__ import annotations
 
-import ctypes as C
 import math
 from dataclasses import dataclass
 from typing import List, Optional, Sequence, Tuple

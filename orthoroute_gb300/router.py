@@ -24,7 +24,6 @@ raises.
 from __future__ import annotations
 
 import heapq
-import math
 import os
 import random
 import time
@@ -36,7 +35,7 @@ import torch
 
 from . import _lib
 from .device import DeviceGraph, DeviceState, Ops, PathStore, require_cuda, route_pass
-from .lattice import Lattice, default_layer_dirs
+from .lattice import Lattice
 
 ROI_THRESHOLD_STEPS = 125
 MAX_ROI_NODES = 50_000
