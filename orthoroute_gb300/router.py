@@ -762,14 +762,15 @@ class PathFinderRouter:
         else:
             dense = getattr(self, "_over_dense", None)
             if dense is None or dense.size != self.E:
-                dense = self._over_dense = np.zeros(self.E, dtype=np.float64)
+                # the over values are float32 on the device: a float32 scratch holds them exactly
+                dense = self._over_dense = np.zeros(self.E, dtype=np.float32)
                 self._over_mask = np.zeros(self.E, dtype=bool)
             mask = self._over_mask
             dense[oi] = ov
             mask[oi] = True
             try:
                 hit = mask[flat]
-                w = dense[flat]
+                w = dense[flat].astype(np.float64)
             finally:
                 dense[oi] = 0.0
                 mask[oi] = False
