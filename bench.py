@@ -33,20 +33,20 @@ if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
 CONFIGS = {
-    # BASELINE configs[0]: 100x100x6, 200 two-pin nets on layer 0, length 5-80, 10 iterations
+    # the CPU-runnable case: 100x100x6, 200 two-pin nets on layer 0, length 5-80, 10 iterations
     "c0": dict(nx=100, ny=100, nz=6, nets=200, iters=10, seed=1234, clusters=False, plain_iters=None),
-    # BASELINE configs[1]: 600x400x12, 2,000 nets, 30% from two 20x20 clusters, <= 40 iterations
+    # the headline case: 600x400x12, 2,000 nets, 30% from two 20x20 clusters, <= 40 iterations
     # plain_iters: the plain one-net-per-launch form is compared on the first iteration only
     # searches_per_job: searches of the (bit-identical) job, used to scale the CPU sample
     "c1": dict(nx=600, ny=400, nz=12, nets=2000, iters=40, seed=4321, clusters=True, via_span=4,
                plain_iters=1, plain_nets=200, searches_per_job=10364,
                # DRAM bytes / algorithmic bytes of full_sssp_kernel, ncu on a 300x200x8 search
                traffic_ratio=0.6655),
-    # BASELINE configs[2]: 600x400x12, 1,500 multi-pin nets (2-16 pins, 1 + geometric(0.35)) with
+    # multi-pin batching: 600x400x12, 1,500 multi-pin nets (2-16 pins, 1 + geometric(0.35)) with
     # pins inside a seeded 50x50 box per net, as star two-pin requests p0 -> pi (multipin.py)
     "c2": dict(nx=600, ny=400, nz=12, nets=1500, iters=40, seed=2468, multipin=True, via_span=4,
                plain_iters=1, plain_nets=300, searches_per_job=52476),
-    # BASELINE configs[3]: 1000x800x32 (25.6 M nodes; 32 layers allow adjacent vias only), a 40x40
+    # BGA escape + backplane: 1000x800x32 (25.6 M nodes; 32 layers allow adjacent vias only), a 40x40
     # BGA at 1 mm (2.5 cells) in the centre and four edge-connector rows; reconciled to 1,600 BGA
     # escape nets (ball -> seeded-random connector pin) + 3,200 backplane nets pairing the other
     # 6,400 connector pins, every pin used once (bga_requests); iterations capped for a run
@@ -334,7 +334,7 @@ def run_ours(args, cfg, rank, world):
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3),
         "higher_is_better": False, "scaling": "weak" if world > 1 else "weak",
         "vs_baseline": None, "dtype": "f32 costs / f64 labels / int32 indices",
-        "data": "synthetic seeded board (BASELINE configs; no dataset)",
+        "data": "synthetic seeded board (seeded nets of the named workload; no dataset)",
         "config": {"workload": args.config, "lattice": [nx, ny, nz], "nets": cfg["nets"],
                    "max_iterations": cfg["iters"], "arcs": router.E, "nodes": router.N,
                    "replicas": "independent per rank" if world > 1 else "single",
