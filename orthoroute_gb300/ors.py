@@ -16,7 +16,7 @@ reference's apart from ``export_timestamp``.
 
 ``import_board_from_orp`` reads and validates a .ORP board file
 (``orp_exporter.py:543-589``).  Routing a board from its pads needs the
-reference's pad escape (portal) planning, which this build does not do;
+reference's pad escape (portal) planning, which this package does not do;
 ``orp_two_pin_requests`` gives the lattice-node tuple requests of an ORP
 file's nets (first two terminals, layer 0) for the tuple-request router.
 """
