@@ -260,3 +260,20 @@ def test_edge_over_sums_match_generator_sums():
         assert sums[i] == sum(float(over_map[e]) for e in edges if e in over_map)
         assert sums[i] == sum(float(over_map.get(e, 0.0)) for e in edges)
         assert bool(hit[i]) == any(e in over_map for e in edges)
+
+
+def test_parse_requests_like_the_reference():
+    """``_parse_requests`` (:4386-4467) for tuples: src == dst is a trivially
+    routed one-node path and no task; non-int endpoints are skipped; nets
+    given by pads raise; and a request list without a task gives the
+    reference's NO-ROUTABLE-NETS result."""
+    h = _router()
+    tasks = h._parse_requests([("A", 3, 9), ("B", 4, 4), ("C", np.int64(1), 2), ("D", 1.0, 2), ("E", 5, 7, 1)])
+    assert tasks == {"A": (3, 9)}
+    assert h.net_paths == {"B": [4]}
+    with pytest.raises(TypeError):
+        h._parse_requests([SimpleNamespace(name="N", pads=[1, 2])])
+    assert R.PathFinderRouter._no_routable_nets([]) == {}
+    res = R.PathFinderRouter._no_routable_nets([("X", 2, 2), ("Y", 1.5, 3)])
+    assert res["error_code"] == "NO-ROUTABLE-NETS" and res["excluded_net_ids"] == ["X", "Y"]
+    assert res["total_nets"] == 2 and not res["success"]
