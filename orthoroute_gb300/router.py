@@ -621,22 +621,6 @@ class PathFinderRouter:
         y, x = divmod(r, self.nx)
         return x, y, z
 
-    def _via_nodes(self, path):
-        """Sorted nodes spanned by the via hops of a path (every layer of each barrel)."""
-        a = np.asarray(path, dtype=np.int64)
-        if a.size < 2:
-            return []
-        z, r = np.divmod(a, self.plane)
-        m = (r[:-1] == r[1:]) & (z[:-1] != z[1:])
-        if not m.any():
-            return []
-        lo = np.minimum(z[:-1], z[1:])[m]
-        cnt = np.maximum(z[:-1], z[1:])[m] - lo + 1
-        rr = r[:-1][m]
-        rep = np.repeat(np.arange(cnt.size), cnt)
-        off = np.arange(int(cnt.sum())) - np.repeat(np.cumsum(cnt) - cnt, cnt)
-        return _sorted_unique((lo[rep] + off) * self.plane + rr[rep]).tolist()
-
     def _overused(self):
         """(arc ids, over values) of every arc with present > capacity (device compaction)."""
         lib = self.ops.lib

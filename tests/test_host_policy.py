@@ -224,20 +224,22 @@ def test_via_pool_members_match_hop_loop(seed):
     assert dict(got) == dict(want)
 
 
-def test_via_nodes_match_hop_loop():
+def test_via_members_match_hop_loop():
+    """Every node spanned by a net's via hops, with the net's id (the flat view)."""
+    from oracle.tallies import via_nodes_for_path
     rng = np.random.default_rng(7)
-    h = _host()
-    for _ in range(50):
+    h = _router()
+    want = set()
+    for i in range(50):
         path = _rand_path(rng, h, int(rng.integers(0, 25)))
-        nodes = set()
-        for u, v in zip(path, path[1:]):
-            zu, ru = divmod(u, h.plane)
-            zv, rv = divmod(v, h.plane)
-            if ru != rv or zu == zv:
-                continue
-            for z in range(min(zu, zv), max(zu, zv) + 1):
-                nodes.add(z * h.plane + ru)
-        assert R.PathFinderRouter._via_nodes(h, path) == sorted(nodes)
+        name = f"N{i}"
+        h.net_paths[name] = path if len(path) >= 2 else []
+        if len(path) >= 2:
+            nid = h._net_id(name)
+            want |= {(n, nid) for n in via_nodes_for_path(path, h.nx, h.plane)}
+    vn, vid = h._flat().via_members()
+    assert set(zip(vn.tolist(), vid.tolist())) == want
+    assert np.all(np.diff(vn) >= 0)
 
 
 def test_edge_over_sums_match_generator_sums():
