@@ -420,6 +420,15 @@ int ogr_full_reuse(int32_t mode, int32_t* current);
  * process-wide, chosen by the autotuner; no reference counterpart. */
 int ogr_search_lanes(int32_t lanes, int32_t* current);
 
+/* How many clashing nets a disjoint-ROI window of ogr_route_pass may skip
+ * to take later nets (0..16, default 8; 0 = consecutive nets only); -1 only
+ * reads.  A later net joins only if its footprint also misses every skipped
+ * net's footprint grown to its fallback ROI bound, and a member that fails
+ * while nets before it are pending is undone and retried in its turn, so
+ * results equal the sequential pass.  Process-wide; no reference
+ * counterpart. */
+int ogr_window_lookahead(int32_t nets, int32_t* current);
+
 /* Tracing of the whole-lattice search (host int64[8], cumulative since the
  * last reset): searches, phases, kernel ns, init ns, E-step work ns and
  * S-step work ns of the busiest CTA, barrier wait ns and statistics +

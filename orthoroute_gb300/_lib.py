@@ -30,7 +30,7 @@ EXPORTED = [
     "ogr_full_profile", "ogr_full_workspace_init", "ogr_find_path_roi", "ogr_reverse_costs",
     "ogr_window_workspace_bytes", "ogr_window_workspace_init", "ogr_window_ctl_bytes",
     "ogr_multi_workspace_bytes", "ogr_find_path_multi", "ogr_full_grid", "ogr_search_lanes",
-    "ogr_paths_commit", "ogr_full_lanes", "ogr_full_reuse",
+    "ogr_paths_commit", "ogr_full_lanes", "ogr_full_reuse", "ogr_window_lookahead",
 ]
 
 P = C.c_void_p
@@ -142,6 +142,7 @@ def load(build_if_missing: bool = True):
         "ogr_search_lanes": [I32, C.POINTER(I32)],
         "ogr_full_lanes": [I32, C.POINTER(I32)],
         "ogr_full_reuse": [I32, C.POINTER(I32)],
+        "ogr_window_lookahead": [I32, C.POINTER(I32)],
         "ogr_paths_commit": [C.POINTER(Graph), C.POINTER(State), P, P, P, I32, P, P, P, P, I32, P, P],
         "ogr_find_path_multi": [C.POINTER(Graph), P, P, I32, P, P, P, I32, P, P, I32, P, C.c_size_t, P, I32,
                                 C.POINTER(I32), P, P],

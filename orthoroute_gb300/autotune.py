@@ -83,6 +83,13 @@ def full_reuse(mode: int = -1) -> int:
     return int(cur.value)
 
 
+def window_lookahead(nets: int = -1) -> int:
+    """Set (0..16) or read (-1) how many clashing nets a disjoint-ROI window may skip."""
+    cur = C.c_int32(0)
+    _lib.check(_lib.load().ogr_window_lookahead(int(nets), C.byref(cur)), "ogr_window_lookahead")
+    return int(cur.value)
+
+
 def cache_path() -> str:
     return os.environ.get("ORTHOROUTE_GB300_TUNE_CACHE",
                           os.path.join(os.path.expanduser("~"), ".cache", "orthoroute_gb300", "autotune.json"))

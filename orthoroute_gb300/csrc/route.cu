@@ -54,6 +54,10 @@ constexpr int kSearchLanes = OGR_SEARCH_LANES;  // default lanes per node of the
 // kernel exists for 2, 4, 8 and 16 lanes; results do not depend on the choice.
 int g_search_lanes = kSearchLanes;
 
+// Nets a disjoint-ROI window may skip over to take later disjoint ones
+// (ogr_window_lookahead; 0 = consecutive nets only).
+int g_window_look = 8;
+
 #define OGR_WITH_LANES(LV, ...)                                \
   do {                                                         \
     switch (g_search_lanes) {                                  \
@@ -67,6 +71,7 @@ constexpr int32_t ST_NONE = 0, ST_FRONT = 1, ST_DONE = 2, ST_SINK = 3;  // SINK:
 constexpr int kMaxViaNodes = 4096;
 constexpr int kDMax = 32;                      // arcs per node the local adjacency holds
 constexpr int kAdjCap = 65536;                 // ROI nodes the local adjacency holds
+constexpr int kMaxSkip = 16;                   // nets a window may skip over (look-ahead)
 
 struct __align__(32) NodeSt {
   double lab;      // FP64 label (tentative until settled)
@@ -1283,14 +1288,15 @@ struct WinSlots {
   int32_t* len;                    // path length of the b-th search
   int32_t* box;                    // [4] footprint box
   unsigned long long* stats;       // [4] the b-th search's statistics, added on acceptance
+  int32_t* inorder;                // 1: no pending net precedes the b-th net
 };
 
 __host__ __device__ inline size_t win_ctl_layout(int32_t slots, char* base, WinCtl** c, WinSlots* s) {
   size_t off = round256(sizeof(WinCtl));
   const size_t k = (size_t)slots;
-  char* p[6];
-  const size_t sz[6] = {4 * k, 4 * k, 4 * k, 4 * k, 16 * k, 32 * k};
-  for (int i = 0; i < 6; ++i) {
+  char* p[7];
+  const size_t sz[7] = {4 * k, 4 * k, 4 * k, 4 * k, 16 * k, 32 * k, 4 * k};
+  for (int i = 0; i < 7; ++i) {
     p[i] = base ? base + off : nullptr;
     off += round256(sz[i]);
   }
@@ -1302,6 +1308,7 @@ __host__ __device__ inline size_t win_ctl_layout(int32_t slots, char* base, WinC
     s->len = (int32_t*)p[3];
     s->box = (int32_t*)p[4];
     s->stats = (unsigned long long*)p[5];
+    s->inorder = (int32_t*)p[6];
   }
   return off;
 }
@@ -1358,12 +1365,13 @@ __device__ int commit_from(const ogr_graph& g, const ogr_state& st, const ogr_ne
 template <int L>
 __global__ void __launch_bounds__(kThreads, 1)
 window_pass_kernel(ogr_graph g, ogr_state st, ogr_net_table t, ogr_pass_args pa, ogr_roi_batch rb, char* slot_base,
-                   size_t slot_bytes, int32_t rmax, int32_t* scratch, char* ctl_base, Ws w) {
+                   size_t slot_bytes, int32_t rmax, int32_t* scratch, char* ctl_base, Ws w, int32_t look) {
   __shared__ Shared sh;
   __shared__ int32_t s_via[kMaxViaNodes];
   __shared__ int s_flags[2];
   __shared__ int s_bar;
   __shared__ int s_box[4];
+  __shared__ int s_skip[4 * kMaxSkip];
   __shared__ int s_win[4];
   WinCtl* c;
   WinSlots ws;
@@ -1377,17 +1385,31 @@ window_pass_kernel(ogr_graph g, ogr_state st, ogr_net_table t, ogr_pass_args pa,
   const int32_t plane = g.nx * g.ny;
   unsigned long long target = 0;
   while (true) {
-    // 1. window formation (CTA 0)
+    // 1. window formation (CTA 0).  Nets are taken in order from the first
+    // pending one while their footprints (ROI box and old-path box) are
+    // pairwise disjoint.  With look > 0 a clashing net is skipped (it stays
+    // pending) and the scan goes on: a later net joins only if it is also
+    // disjoint from every skipped net's footprint grown to the bound of its
+    // fallback ROI (terminals +- fallback BFS depth + halo), so it commutes
+    // with the skipped nets whatever they do when their turn comes.
+    // Pending = net_status still -1 (set before the launch).
     if (b == 0) {
-      if (tid == 0) { s_win[0] = c->cursor; s_win[1] = 0; }
+      if (tid == 0) {
+        int cur = c->cursor;
+        while (cur < pa.count && pa.net_status[cur] != -1) ++cur;
+        c->cursor = cur;
+        s_win[0] = cur;
+      }
       __syncthreads();
-      int k = s_win[0], W = 0;
-      while (k < pa.count && W < G) {
+      const int k0 = s_win[0];
+      int W = 0, nskip = 0;
+      for (int k = k0; k < pa.count && W < G && k - k0 < 4 * G; ++k) {
+        if (*(volatile int32_t*)&pa.net_status[k] != -1) continue;   // done out of order earlier
         const int32_t n = pa.order[k];
         const int32_t R = rb.roi_len[n];
         if (R <= 0) {
-          if (W == 0) {
-            if (tid == 0) { ws.k[0] = k; ws.solo[0] = 1; }
+          if (W == 0 && nskip == 0) {
+            if (tid == 0) { ws.k[0] = k; ws.solo[0] = 1; ws.inorder[0] = 1; }
             W = 1;
           }
           break;
@@ -1407,15 +1429,31 @@ window_pass_kernel(ogr_graph g, ogr_state st, ogr_net_table t, ogr_pass_args pa,
         __syncthreads();
         bool clash = false;
         for (int m = 0; m < W && !clash; ++m) clash = boxes_meet(s_box, ws.box + 4 * m);
-        if (clash) break;
+        for (int q = 0; q < nskip && !clash; ++q) clash = boxes_meet(s_box, s_skip + 4 * q);
+        if (clash) {
+          if (nskip >= look) break;   // no look-ahead left: the window ends here
+          if (tid == 0) {
+            const int32_t sr = t.net_src[n] % plane, dr = t.net_dst[n] % plane;
+            const int sx = sr % g.nx, sy = sr / g.nx, dx = dr % g.nx, dy = dr / g.nx;
+            const int m = t.net_depth[2 * n + 1] + t.net_halo[2 * n + 1];
+            int* q = s_skip + 4 * nskip;
+            q[0] = min(s_box[0], min(sx, dx) - m);
+            q[1] = max(s_box[1], max(sx, dx) + m);
+            q[2] = min(s_box[2], min(sy, dy) - m);
+            q[3] = max(s_box[3], max(sy, dy) + m);
+          }
+          __syncthreads();
+          ++nskip;
+          continue;
+        }
         if (tid == 0) {
           ws.k[W] = k;
           ws.solo[W] = 0;
+          ws.inorder[W] = nskip == 0 ? 1 : 0;
           for (int q = 0; q < 4; ++q) ws.box[4 * W + q] = s_box[q];
         }
         __syncthreads();
         ++W;
-        ++k;
       }
       if (tid == 0) c->wsize = W;
     }
@@ -1469,7 +1507,6 @@ window_pass_kernel(ogr_graph g, ogr_state st, ogr_net_table t, ogr_pass_args pa,
         if (tid == 0) {
           pa.net_status[k] = 0;
           if (rc != OGR_OK) atomicExch(&c->error, rc);
-          if (b == W - 1) c->cursor = k + 1;
         }
       }
     } else if (b == 0) {
@@ -1481,7 +1518,11 @@ window_pass_kernel(ogr_graph g, ogr_state st, ogr_net_table t, ogr_pass_args pa,
         if (tid == 0) pa.net_status[k] = 0;
         __syncthreads();
       }
-      for (int m = ff + 1; m < W && rc == OGR_OK; ++m) {   // undo the later rip-ups
+      // A failed net with pending nets before it (taken out of order) must
+      // not take its fallback yet: it is undone like the later members and
+      // stays pending, to be searched again when its turn comes.
+      const bool defer = !ws.inorder[ff];
+      for (int m = defer ? ff : ff + 1; m < W && rc == OGR_OK; ++m) {   // undo the later rip-ups
         const int32_t n = pa.order[ws.k[m]];
         const int32_t ol = t.store_len[n];
         if (ol >= 2)
@@ -1489,6 +1530,9 @@ window_pass_kernel(ogr_graph g, ogr_state st, ogr_net_table t, ogr_pass_args pa,
                               pa.live, nullptr, s_via, s_flags);
       }
       const int32_t kf = ws.k[ff], nf = pa.order[kf];
+      if (defer) {
+        if (tid == 0 && rc != OGR_OK) atomicExch(&c->error, rc);
+      } else {
       if (tid < 4) atomicAdd(&stats[tid], ws.stats[4 * ff + tid]);
       if (tid == 0) t.store_len[nf] = 0;
       __syncthreads();
@@ -1513,8 +1557,8 @@ window_pass_kernel(ogr_graph g, ogr_state st, ogr_net_table t, ogr_pass_args pa,
       }
       if (tid == 0) {
         pa.net_status[kf] = flags;
-        c->cursor = kf + 1;
         if (rc != OGR_OK) atomicExch(&c->error, rc);
+      }
       }
     }
     if (!win_barrier(c, target, &s_bar)) break;
@@ -1634,6 +1678,13 @@ extern "C" int ogr_window_workspace_init(void* ws, int32_t num_nodes, int32_t ma
 }
 
 extern "C" size_t ogr_window_ctl_bytes(int32_t slots) { return win_ctl_layout(slots, nullptr, nullptr, nullptr); }
+
+extern "C" int ogr_window_lookahead(int32_t nets, int32_t* current) {
+  if (nets < -1 || nets > kMaxSkip) return OGR_ERR_ARG;
+  if (nets >= 0) g_window_look = nets;
+  if (current) *current = g_window_look;
+  return OGR_OK;
+}
 
 extern "C" int ogr_search_lanes(int32_t lanes, int32_t* current) {
   if (lanes != 0 && lanes != 2 && lanes != 4 && lanes != 8 && lanes != 16) return OGR_ERR_ARG;
@@ -1874,6 +1925,9 @@ extern "C" int ogr_route_pass(const ogr_graph* g, const ogr_state* st, const ogr
       return OGR_OK;
     }
     OGR_CUDA_TRY(cudaMemsetAsync(win->ctl, 0, ogr_window_ctl_bytes(grid), s));
+    // every net of the segment starts pending (-1); the window pass sets its status when done
+    OGR_CUDA_TRY(cudaMemsetAsync(seg.net_status, 0xff, sizeof(int32_t) * (size_t)seg.count, s));
+    int32_t lookv = g_window_look < 0 ? 0 : (g_window_look > kMaxSkip ? kMaxSkip : g_window_look);
     ogr_graph gv = *g;
     ogr_state sv = *st;
     ogr_net_table tv = *t;
@@ -1884,7 +1938,7 @@ extern "C" int ogr_route_pass(const ogr_graph* g, const ogr_state* st, const ogr
     int32_t* scratch = win->scratch;
     char* ctl = (char*)win->ctl;
     Ws wv = w;
-    void* args[] = {&gv, &sv, &tv, &pv, &rbv, &slot_base, &slot_bytes, &rmax, &scratch, &ctl, &wv};
+    void* args[] = {&gv, &sv, &tv, &pv, &rbv, &slot_base, &slot_bytes, &rmax, &scratch, &ctl, &wv, &lookv};
     const void* wk = nullptr;
     OGR_WITH_LANES(L, wk = (const void*)window_pass_kernel<L>);
     OGR_CUDA_TRY(cudaLaunchCooperativeKernel(wk, dim3(grid), dim3(kThreads), args, 0,

@@ -61,16 +61,20 @@ def _run(window_slots, seed):
     return out, state
 
 
-@pytest.mark.parametrize("seed,lanes", [(3, 4), (11, 4), (3, 2)])
-def test_windows_match_sequential_pass(seed, lanes):
-    from orthoroute_gb300.autotune import search_lanes
-    before = search_lanes(0)
+@pytest.mark.parametrize("seed,lanes,look", [(3, 4, 8), (11, 4, 8), (3, 2, 16), (11, 4, 0)])
+def test_windows_match_sequential_pass(seed, lanes, look):
+    """look > 0: windows skip clashing nets and take later disjoint ones (failed
+    out-of-order members are undone and retried in turn); 0: consecutive only."""
+    from orthoroute_gb300.autotune import search_lanes, window_lookahead
+    before, look0 = search_lanes(0), window_lookahead()
     try:
         search_lanes(lanes)
+        window_lookahead(look)
         seq, seq_state = _run(0, seed)
         win, win_state = _run(16, seed)
     finally:
         search_lanes(before)
+        window_lookahead(look0)
     failed = 0
     for (s0, st0, l0, p0, a0), (s1, st1, l1, p1, a1) in zip(seq, win):
         np.testing.assert_array_equal(s0, s1)
