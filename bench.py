@@ -405,8 +405,11 @@ def cpu_job_sample(cfg, budget_s=20.0, searches_hint=None):
     dt = time.perf_counter() - t1
     per = dt / max(1, R.stats["searches"])
     n = cfg["searches_per_job"] or searches_hint
+    how = "searches per job"
+    if not n:   # no measured count: one search per net and iteration (an estimate)
+        n, how = len(tasks) * cfg["iters"], "searches per job (estimated: nets x iterations)"
     return per * n, (f"{R.stats['searches']} searches of iteration 1 ({len(sample)} nets, {dt:.1f} s, "
-                     f"{per:.3f} s/search) x {n} searches per job; host policy time excluded"), 1
+                     f"{per:.3f} s/search) x {n} {how}; host policy time excluded"), 1
 
 
 def run_reference(args, cfg):
