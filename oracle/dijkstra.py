@@ -165,7 +165,7 @@ def _clib():
         lib = ctypes.CDLL(_b.build())
         P = ctypes.c_void_p
         lib.oracle_heap_dijkstra.argtypes = [ctypes.c_int32, ctypes.c_int32, P, P, P, P, ctypes.c_int32, P, P, P,
-                                             ctypes.POINTER(ctypes.c_int32), P]
+                                             ctypes.POINTER(ctypes.c_int32), P, ctypes.c_int32]
         lib.oracle_heap_dijkstra.restype = ctypes.c_int
         _CLIB = lib
     return _CLIB
@@ -188,7 +188,7 @@ def find_path_roi_c(indptr, indices, src, dst, costs, roi_nodes, global_to_roi, 
     rc = lib.oracle_heap_dijkstra(int(src), int(dst), ip.ctypes.data, ix.ctypes.data, c.ctypes.data,
                                   roi.ctypes.data, len(roi), g2r.ctypes.data,
                                   None if pen is None else pen.ctypes.data, out.ctypes.data, ctypes.byref(n),
-                                  st.ctypes.data)
+                                  st.ctypes.data, len(ip) - 1)
     if rc < 0:
         raise MemoryError("oracle heap Dijkstra allocation failed")
     if stats is not None:
