@@ -976,6 +976,8 @@ class PathFinderRouter:
         roi_nets = autotune.sample_roi_nets(tasks, self._manhattan, ROI_THRESHOLD_STEPS)
         self.tuning = autotune.tune(self.ops, self.lattice, nets, roi_nets)
         self.full_engine = self.tuning.full_engine
+        # the timing searches added to the device counters; the job's own start at zero
+        self.ops.stats.zero_()
 
     def _route_all(self, tasks, all_tasks):
         cfg = self.config

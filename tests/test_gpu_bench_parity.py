@@ -91,7 +91,9 @@ def test_c0_matches_oracle_loop_in_process(mode, tmp_path, monkeypatch):
     ores = O.route({n: (s, d) for n, s, d in reqs})
     assert first_difference(R.trace.records, O.trace.records) is None
     assert len(R.trace) == len(O.trace)
-    assert [dict(m) for m in res["iteration_metrics"]] == [dict(m) for m in ores["iteration_metrics"]]
+    assert len(res["iteration_metrics"]) == len(ores["iteration_metrics"])
+    for a, b in zip(res["iteration_metrics"], ores["iteration_metrics"]):
+        assert {k: a[k] for k in b} == b
     for k in ("success", "barrel_conflicts", "overuse_sum", "failed_nets"):
         if k in ores and k in res:
             assert res[k] == ores[k], k
