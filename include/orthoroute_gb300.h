@@ -414,6 +414,27 @@ int ogr_full_lanes(int32_t lanes, int32_t* current);
  * reference counterpart. */
 int ogr_full_reuse(int32_t mode, int32_t* current);
 
+/* Engine of the whole-lattice search for searches launched afterwards:
+ * enable = 1 selects the tile-window engine with window width `delta`
+ * (label units, > 0) and tiles of tx x ty cells over all layers (0: sized
+ * from the lattice to fit shared memory); enable = 0 keeps the
+ * phase-settled engine; -1 only reads (*cur_enable, *cur_delta, host, may be
+ * NULL).  The tile engine computes the same fixed point with many hops per
+ * grid step; a net it cannot take (a cost or penalty below 2^-7, a label
+ * of 2^23 or more, a tile over capacity, an iteration cap) is searched by
+ * the phase engine in the same stream, so results, statistics and status
+ * codes do not depend on this setting.  Process-wide, chosen by the
+ * autotuner; the window width is the delta of a delta-stepping search; no
+ * reference counterpart. */
+int ogr_full_tile(int32_t enable, double delta, int32_t tx, int32_t ty, int32_t* cur_enable,
+                  double* cur_delta);
+
+/* Tracing of the tile-window engine (host int64[8], cumulative since the
+ * last reset): searches, grid rounds, windows, kernel ns, searches handed to
+ * the phase engine, bit set of the reasons for handing over, local
+ * iterations, tile processings.  Synchronous. */
+int ogr_tile_profile(int64_t* out8, int32_t reset);
+
 /* Lanes per node of the single-CTA ROI search (2, 4, 8 or 16; default 4) for
  * every search launched afterwards; 0 only reads.  *current (host, may be
  * NULL) receives the setting.  A tuning knob (results do not depend on it),

@@ -2,12 +2,14 @@
 
 Full-graph nets (Manhattan length >= 125, ``_route_all`` :8219-8262) are
 searched either by ``full_sssp_kernel`` on a cooperative grid of CTAs (one
-grid step per settle phase) or by a single 1024-thread CTA.  Which one is
-faster, and with how many CTAs, depends on the lattice: a grid step costs a
-grid-wide barrier (more CTAs, dearer barrier) and spreads the phase's front
-over the CTAs (more CTAs, less work each).  The exact search has no bucket
-width to tune: each phase's threshold is the least tentative label, and the
-settle rule is fixed by exactness.  So the tuner sweeps
+grid step per settle phase), by the tile-window engine on a grid of one CTA
+per SM, or by a single 1024-thread CTA.  Which one is faster, and with how
+many CTAs, depends on the lattice: a grid step costs a grid-wide barrier
+(more CTAs, dearer barrier) and spreads the phase's front over the CTAs
+(more CTAs, less work each).  The phase engine has no bucket width to tune
+(each phase's threshold is the least tentative label and the settle rule is
+fixed by exactness); the tile-window engine's window width is one.  So the
+tuner sweeps
 
 * the engine: "grid" or "cta";
 * the lanes per examined frontier node of the "grid" engine (4, 8, 16) and
@@ -15,6 +17,9 @@ settle rule is fixed by exactness.  So the tuner sweeps
   the full grid;
 * then the grid of the "grid" engine: 1/4, 1/2, 3/4 and all of the resident
   CTAs (SMs x CTAs per SM);
+* then the tile-window engine (label windows over lattice tiles in shared
+  memory, tilesearch.cu) at window widths delta of 2, 4, 8, 16 and 32
+  uncongested lateral hops: the delta of a delta-stepping search;
 
 on a few full-graph searches of the job's own long nets over the current
 costs, and keeps the fastest.  For ROI nets (one 1024-thread CTA per search)
@@ -47,6 +52,7 @@ class Tuning:
     roi_lanes: int = 4
     full_lanes: int = 16
     full_reuse: int = 0
+    full_tile_delta: float = 0.0     # > 0: tile-window engine with this window width
     samples: int = 0
     cached: bool = False
 
@@ -81,6 +87,24 @@ def full_reuse(mode: int = -1) -> int:
     cur = C.c_int32(0)
     _lib.check(_lib.load().ogr_full_reuse(int(mode), C.byref(cur)), "ogr_full_reuse")
     return int(cur.value)
+
+
+TILE_DELTA_HOPS = (2, 4, 8, 16, 32)
+
+
+def full_tile(enable: int = -1, delta: float = 0.0, tx: int = 0, ty: int = 0) -> Tuple[int, float]:
+    """Select (enable 1 with window width delta > 0), deselect (0) or read (-1)
+    the tile-window engine of whole-lattice searches: (enabled, delta)."""
+    cur, d = C.c_int32(0), C.c_double(0.0)
+    _lib.check(_lib.load().ogr_full_tile(int(enable), float(delta), int(tx), int(ty), C.byref(cur), C.byref(d)),
+               "ogr_full_tile")
+    return int(cur.value), float(d.value)
+
+
+def hop_cost(lattice, base_cost_weight: float = 0.3) -> float:
+    """One uncongested lateral hop of the cost update (pitch x base weight):
+    the unit of the tile engine's window widths."""
+    return float(lattice.pitch) * float(base_cost_weight)
 
 
 def window_lookahead(nets: int = -1) -> int:
@@ -152,9 +176,11 @@ def tune(ops, lattice, nets: Sequence[Tuple[int, int]], roi_nets: Sequence[Tuple
                 full_grid(t.full_ctas)
                 full_lanes(t.full_lanes)
                 full_reuse(t.full_reuse)
+            full_tile(1 if t.full_tile_delta > 0 else 0, t.full_tile_delta)
             search_lanes(t.roi_lanes)
             return t
     cur, limit = full_grid(0)
+    full_tile(0)
     nets = list(nets)
     roi_nets = list(roi_nets)
     timings: Dict[str, float] = {}
@@ -211,11 +237,26 @@ def tune(ops, lattice, nets: Sequence[Tuple[int, int]], roi_nets: Sequence[Tuple
                 best = (engine, ctas, ms)
     finally:
         stream.synchronize()
-    engine, ctas, _ = best
+    engine, ctas, best_ms = best
     full_grid(ctas if engine == "grid" else cur)
+    # the tile-window engine at each window width (it hands a net it cannot
+    # take to the phase engine configured above)
+    tile_delta = 0.0
+    if engine == "grid":
+        unit = hop_cost(lattice)
+        try:
+            for hops in TILE_DELTA_HOPS:
+                full_tile(1, hops * unit)
+                ms = time_full("grid")
+                timings[f"tile_delta{hops}"] = round(ms, 4)
+                if ms < best_ms:
+                    best_ms, tile_delta = ms, hops * unit
+        finally:
+            full_tile(1 if tile_delta > 0 else 0, tile_delta)
+            stream.synchronize()
     t = Tuning(key=key, full_engine=engine, full_ctas=ctas if engine == "grid" else cur, ms_per_search=timings,
                samples=len(nets) + len(roi_nets), roi_lanes=best_lanes, full_lanes=best_full_lanes,
-               full_reuse=best_reuse)
+               full_reuse=best_reuse, full_tile_delta=tile_delta)
     if use_cache:
         _store_cache(path, key, t)
     return t

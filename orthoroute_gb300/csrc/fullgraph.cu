@@ -55,6 +55,7 @@ struct FCtl {
   alignas(128) int32_t nlog;                   // settled-log length
   alignas(128) int32_t res[4];
   int32_t gbase;                               // persistent across searches
+  int32_t tile_gate;                           // 1: the tile engine handed this net over
 };
 
 // Per-node search record: label, settle stamp, reach stamp in one 16-byte
@@ -81,6 +82,7 @@ struct FWs {
   FEntry* fr[3];             // frontier lists: read, write, and the one being cleared
   int32_t* log;              // settled nodes in settle order
   FCtl* ctl;
+  char* tile;                // scratch of the tile-window engine
 };
 
 constexpr size_t r256(size_t v) { return (v + 255) & ~(size_t)255; }
@@ -102,6 +104,7 @@ size_t fws_layout(int32_t N, int64_t E, char* base, FWs* w) {
   t.rcost = (float*)take(4 * (size_t)E);
   for (int i = 0; i < 3; ++i) t.fr[i] = (FEntry*)take(16 * n);
   t.log = (int32_t*)take(4 * n);
+  t.tile = take(ogr_tile::workspace_bytes(N));
   if (w) *w = t;
   return off;
 }
@@ -250,6 +253,7 @@ full_sssp_kernel(ogr_graph g, ogr_state st, ogr_full::Job job, FWs w) {
   FCtl* ctl = w.ctl;
 
   if (job.from_pass && job.pass_result[0] < 0) return;  // uniform: written by an earlier launch
+  if (job.gated && __ldcg(&ctl->tile_gate) == 0) return;  // uniform: the tile engine found the result
   ogr_net_args a = job.a;
   int32_t* path_out = job.path_out;
   int32_t path_cap = job.path_cap;
@@ -606,11 +610,19 @@ int launch(const ogr_graph& g, const ogr_state& st, const Job& job, void* ws, cu
   FWs w;
   fws_layout(g.num_nodes, g.num_edges, (char*)ws, &w);
   w.reuse = g_full_reuse;
+  ogr_full::Job jv = job;
+  jv.gated = 0;
+  if (ogr_tile::enabled()) {
+    const int trc = ogr_tile::launch(g, st, job, w.tile, w.ctl->res, &w.ctl->tile_gate, s);
+    if (trc == OGR_OK)
+      jv.gated = 1;              // the phase engine runs only if the net was handed over
+    else if (trc != OGR_ERR_CAPACITY)
+      return trc;                // (capacity: this lattice does not tile; phase engine alone)
+  }
   // bar_count, bar_gen and bar_err start at zero on every launch
   OGR_CUDA_TRY(cudaMemsetAsync(w.ctl, 0, offsetof(FCtl, tbits), s));
   ogr_graph gv = g;
   ogr_state sv = st;
-  ogr_full::Job jv = job;
   void* args[] = {&gv, &sv, &jv, &w};
   const void* fn = g_full_lanes == 4   ? (const void*)full_sssp_kernel<4>
                    : g_full_lanes == 8 ? (const void*)full_sssp_kernel<8>
@@ -658,8 +670,10 @@ extern "C" int ogr_full_workspace_init(void* ws, size_t bytes, int32_t num_nodes
   if (bytes < ogr_full::workspace_bytes(num_nodes, num_edges)) return OGR_ERR_CAPACITY;
   FWs w;
   fws_layout(num_nodes, num_edges, (char*)ws, &w);
-  // phase base 0: the first search clears the settle stamps
+  // phase base 0: the first search clears the settle stamps; tile stamp 0:
+  // the first tile search clears its node words
   OGR_CUDA_TRY(cudaMemsetAsync(w.ctl, 0, sizeof(FCtl), ogr_stream(stream)));
+  OGR_CUDA_TRY(cudaMemsetAsync(w.tile, 0, ogr_tile::ctl_bytes(), ogr_stream(stream)));
   return OGR_OK;
 }
 

@@ -384,14 +384,16 @@ class PathFinderRouter:
         require_cuda()
         if mode not in ("persistent", "plain"):
             raise ValueError("mode must be 'persistent' (one launch per routing pass) or 'plain' (one per net)")
-        if full_engine not in ("grid", "cta", "auto"):
-            raise ValueError("full_engine must be 'grid' (all SMs per full-graph net), 'cta' (one CTA) or "
+        if full_engine not in ("grid", "tile", "cta", "auto"):
+            raise ValueError("full_engine must be 'grid' (phase-settled search on all SMs per full-graph net), "
+                             "'tile' (tile-window search on all SMs), 'cta' (one CTA) or "
                              "'auto' (the autotuner picks per lattice)")
         self.config = config or PathFinderConfig()
         self.device = device
         self.mode = mode
-        self.full_engine = full_engine
+        self.full_engine = "grid" if full_engine == "tile" else full_engine
         self.full_engine_request = full_engine
+        self.full_tile_delta = 0.0       # > 0: whole-lattice searches use the tile-window engine
         self.tuning = None
         self.window_slots = int(window_slots)   # > 0: batched disjoint-ROI windows in persistent mode
         self.store: Optional[PathStore] = None
@@ -500,6 +502,9 @@ class PathFinderRouter:
         self.tuning = None
         if self.full_engine_request == "auto":
             self.full_engine = "grid"
+        from . import autotune
+        self.full_tile_delta = (autotune.TILE_DELTA_HOPS[2] * autotune.hop_cost(lattice, self.config.base_cost_weight)
+                                if self.full_engine_request == "tile" else 0.0)
         # copper layer names as initialize_graph derives them (:2883-2904)
         names = list(layer_names) if layer_names else list(getattr(self.config, "layer_names", []) or [])
         if len(names) != lattice.nz:
@@ -976,6 +981,7 @@ class PathFinderRouter:
         roi_nets = autotune.sample_roi_nets(tasks, self._manhattan, ROI_THRESHOLD_STEPS)
         self.tuning = autotune.tune(self.ops, self.lattice, nets, roi_nets)
         self.full_engine = self.tuning.full_engine
+        self.full_tile_delta = self.tuning.full_tile_delta
         # the timing searches added to the device counters; the job's own start at zero
         self.ops.stats.zero_()
 
@@ -989,6 +995,9 @@ class PathFinderRouter:
             self.ops.live_begin(self._present_pres_fac)
         if self.full_engine_request == "auto" and self.tuning is None:
             self._autotune(all_tasks)
+        # the engine knob is process-wide: every pass sets this router's choice
+        from . import autotune
+        autotune.full_tile(1 if self.full_tile_delta > 0 else 0, self.full_tile_delta)
         if self.mode == "persistent":
             return self._route_all_pass(tasks, all_tasks, ordered, bonus, live)
         for name in ordered:
