@@ -429,11 +429,14 @@ int ogr_full_reuse(int32_t mode, int32_t* current);
 int ogr_full_tile(int32_t enable, double delta, int32_t tx, int32_t ty, int32_t* cur_enable,
                   double* cur_delta);
 
-/* Tracing of the tile-window engine (host int64[8], cumulative since the
+/* Tracing of the tile-window engine (host int64[24], cumulative since the
  * last reset): searches, grid rounds, windows, kernel ns, searches handed to
  * the phase engine, bit set of the reasons for handing over, local
- * iterations, tile processings.  Synchronous. */
-int ogr_tile_profile(int64_t* out8, int32_t reset);
+ * iterations, tile processings; ns summed over CTAs spent loading tile
+ * structure, loading labels, iterating and writing back, and waiting at grid
+ * barriers; structure loads; the most tiles one CTA took in a round; node
+ * evaluations; ns of first sweeps.  Synchronous. */
+int ogr_tile_profile(int64_t* out24, int32_t reset);
 
 /* Lanes per node of the single-CTA ROI search (2, 4, 8 or 16; default 4) for
  * every search launched afterwards; 0 only reads.  *current (host, may be

@@ -47,8 +47,12 @@ namespace ogr_tile {
 // Tracing counters (ogr_tile_profile): [0] searches, [1] grid rounds,
 // [2] windows, [3] kernel ns, [4] searches handed to the phase engine,
 // [5] bit set of the reasons for handing over (1 << kWhy*), [6] local
-// iterations, [7] tile processings.
-__device__ unsigned long long g_tile_prof[8];
+// iterations, [7] tile processings; per-stage globaltimer ns summed over the
+// CTAs: [8] structure loads, [9] label loads, [10] local iterations,
+// [11] write-back, [12] barrier waits; [13] structure loads, [14] most
+// tiles one CTA processed in a round, [15] node evaluations, [16] ns of
+// first sweeps.
+__device__ unsigned long long g_tile_prof[24];
 }  // namespace ogr_tile
 
 namespace {
@@ -59,7 +63,6 @@ constexpr int kMaxArcs = 18432;                  // arcs of a tile's rows
 constexpr int kMaxHalo = 1024;                   // ring cells around a tile (all layers)
 constexpr int kMaxTiles = 65536;                 // tiles of a lattice (else: phase engine)
 constexpr int kMaxOwn = 512;                     // tiles of one CTA listed in a round
-constexpr int kTickBits = 30;
 constexpr long long kInf = (1LL << 53) - 1;      // "no label"
 constexpr unsigned long long kTickMask = (1ULL << 53) - 1;
 constexpr int kStampMax = 2047;                  // 11-bit search stamp, 0 = never valid
@@ -136,6 +139,7 @@ struct Sm {
   float acost[kMaxArcs];                 // cost of the arc in-neighbour -> node
   int32_t hgid[kMaxHalo];                // global id of each ring slot (-1: off the lattice)
   int32_t gid[kMaxNodes];                // global id of each tile node
+  int32_t f0[kMaxNodes];                 // global CSR row start of each tile node
   uint32_t rmask[kMaxNodes / 8];         // 4 bits per node: ring sides (W, E, S, N) its arcs reach
   uint32_t wl[2][kMaxNodes / 32];        // worklists
   uint32_t chg[kMaxNodes / 32];          // label or winner changed since the load
@@ -196,10 +200,24 @@ __device__ __forceinline__ bool f32_ticks(float v, long long& t) {
   return true;
 }
 
-// float32 of a label given in ticks (exact scaling of the int64 rounding).
-__device__ __forceinline__ float ticks_f32(long long t) {
-  static_assert(kTickBits == 30, "the scale below is 2^-kTickBits");
-  return __ll2float_rn(t) * 0x1p-30f;
+// The largest tick count whose float32 rounding (x 2^-30, to nearest, ties
+// to even; 30 - 23 = 7 is not needed here, only the mantissa spacing) equals
+// that of t, from integer operations.  t >= 1.
+__device__ __forceinline__ long long round_hi(long long t) {
+  const unsigned long long u = (unsigned long long)t;
+  const int nb = 64 - __clzll(u);
+  if (nb <= 24) return t;                    // exact: no other integer rounds to it
+  const int sh = nb - 24;
+  unsigned long long m = u >> sh;
+  const unsigned long long rem = u & ((1ull << sh) - 1ull);
+  const unsigned long long half = 1ull << (sh - 1);
+  if (rem > half || (rem == half && (m & 1ull))) ++m;
+  int e = sh;
+  if (m == (1ull << 24)) {
+    m >>= 1;
+    ++e;
+  }
+  return (long long)((m << e) + (1ull << (e - 1)) - (m & 1ull));
 }
 
 // Grid barrier on a monotone arrival counter (bounded wait; false when any
@@ -278,7 +296,7 @@ __device__ int block_scan(Sm& sm, int v, int& excl) {
 // a penalty is off the exact grid.
 __device__ bool load_structure(Sm& sm, const Geo& G, int t, int32_t src, const ogr_graph& g,
                                const ogr_state& st, const ogr_net_args& a, TCtl* ctl) {
-  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  const int tid = threadIdx.x;
   if (tid == 0) {
     const int tyi = t / G.ntx, txi = t - tyi * G.ntx;
     sm.x0 = txi * G.tx;
@@ -311,7 +329,9 @@ __device__ bool load_structure(Sm& sm, const Geo& G, int t, int32_t src, const o
       const int z = c / th, ly = c - z * th;
       const int32_t gid = (int32_t)((int64_t)z * G.plane + (int64_t)(y0 + ly) * G.nx + x0 + lx);
       sm.gid[i] = gid;
-      deg[k] = g.indptr[gid + 1] - g.indptr[gid];
+      const int32_t r0 = g.indptr[gid];
+      sm.f0[i] = r0;
+      deg[k] = g.indptr[gid + 1] - r0;
       long long pt;
       if (!f32_ticks(ogr_node_penalty(st, a, gid), pt)) badpen = true;
       sm.pen[i] = pt;
@@ -348,13 +368,14 @@ __device__ bool load_structure(Sm& sm, const Geo& G, int t, int32_t src, const o
   }
   __syncthreads();
   // arcs, one warp per row chunk
+  const int lane = tid & 31, wid = tid >> 5;
   bool bad = false;
   const int nchunks = th * G.nz;
   for (int c = wid; c < nchunks; c += kT / 32) {
     const int i0 = c * tw;
     const int z = c / th, ly = c - z * th;
     const int l0 = sm.rs[i0], l1 = sm.rs[i0 + tw];
-    const int64_t gf0 = g.indptr[sm.gid[i0]];      // same address on every lane
+    const int64_t gf0 = sm.f0[i0];
     for (int e = l0 + lane; e < l1; e += 32) {
       const int64_t f = gf0 + (e - l0);
       const int32_t u = g.indices[f];
@@ -366,12 +387,12 @@ __device__ bool load_structure(Sm& sm, const Geo& G, int t, int32_t src, const o
         else hi = mid;
       }
       const int i = lo, lx = i - i0;
-      const int64_t d = (int64_t)u - sm.gid[i];
+      const int d = u - sm.gid[i];
       int slot = -1, side = -1;
       if (G.nx > 1 && (d == 1 || d == -1)) {
-        const int nlx = lx + (int)d;
+        const int nlx = lx + d;
         if (nlx >= 0 && nlx < tw) {
-          slot = i + (int)d;
+          slot = i + d;
         } else {
           side = d < 0 ? 0 : 1;
           slot = nt + (side * G.nz + z) * G.tm + ly;
@@ -386,7 +407,7 @@ __device__ bool load_structure(Sm& sm, const Geo& G, int t, int32_t src, const o
         }
       } else {
         const int dz = __float2int_rn((float)d * G.inv_plane);
-        if ((int64_t)dz * G.plane == d && z + dz >= 0 && z + dz < G.nz) slot = i + dz * tw * th;
+        if ((int64_t)dz * G.plane == (int64_t)d && z + dz >= 0 && z + dz < G.nz) slot = i + dz * tw * th;
       }
       if (slot < 0 || slot_gid(sm, slot) != u) {   // not a lattice step of this tile or its ring
         bad = true;
@@ -426,8 +447,15 @@ __device__ bool process_tile(Sm& sm, const Geo& G, int t, const ogr_graph& g, co
                              const ogr_net_args& a, const TWs& w, unsigned stamp, int32_t src, long long wstart,
                              long long B, int rnext, uint32_t gnext, int wb) {
   const int tid = threadIdx.x;
+  unsigned long long tm0 = tid == 0 ? gtimer() : 0;
   if (sm.cached != t) {
     if (!load_structure(sm, G, t, src, g, st, a, w.ctl)) return false;
+    if (tid == 0) {
+      const unsigned long long t1 = gtimer();
+      atomicAdd(&ogr_tile::g_tile_prof[8], t1 - tm0);
+      atomicAdd(&ogr_tile::g_tile_prof[13], 1ull);
+      tm0 = t1;
+    }
   }
   const int nt = sm.nt;
   const int nh = 4 * G.nz * G.tm;
@@ -444,9 +472,7 @@ __device__ bool process_tile(Sm& sm, const Geo& G, int t, const ogr_graph& g, co
     sm.lab[nt + h] = gid >= 0 ? word_ticks(ld_word(&w.word[gid]), stamp) : kInf;
   }
   for (int k = tid; k < nwords; k += kT) {
-    // first sweep: every node; the rest follow label changes
-    const int rem = nt - 32 * k;
-    sm.wl[0][k] = rem >= 32 ? 0xffffffffu : ((1u << rem) - 1u);
+    sm.wl[0][k] = 0u;
     sm.wl[1][k] = 0u;
     sm.chg[k] = 0u;
     sm.lchg[k] = 0u;
@@ -454,6 +480,18 @@ __device__ bool process_tile(Sm& sm, const Geo& G, int t, const ogr_graph& g, co
   if (tid < 4) sm.sidemark[tid] = 0;
   if (tid == 0) sm.flag = 1;
   __syncthreads();
+  if (tid == 0) {
+    const unsigned long long t1 = gtimer();
+    atomicAdd(&ogr_tile::g_tile_prof[9], t1 - tm0);
+    tm0 = t1;
+  }
+  // Iteration 0 evaluates every node; iteration k evaluates the nodes with
+  // an in-tile in-neighbour whose label changed in iteration k - 1 (the
+  // bitmap wl[prev], pulled, so no two threads write one word).  Node
+  // i = base + tid: a warp owns one 32-bit word of every bitmap and writes it
+  // from a ballot.  One barrier per iteration.
+  const int lane = tid & 31, wid = tid >> 5;
+  unsigned nev_all = 0;
   int cur = 0;
   const int cap = 4 * nt + 64;
   int it = 0;
@@ -462,86 +500,125 @@ __device__ bool process_tile(Sm& sm, const Geo& G, int t, const ogr_graph& g, co
       if (tid == 0) fail(w.ctl, kWhyLocalCap);
       return false;
     }
+    const int prev = cur ^ 1;
     bool changed = false, bad = false;
-    for_my_nodes(nt, [&](int i) {
-      if (!((sm.wl[cur][i >> 5] >> (i & 31)) & 1u)) return;
-      const long long li = sm.lab[i];
-      if (li < wstart) return;                      // final since an earlier window
-      if (i == sm.srcl) return;                     // the source keeps label 0
-      const long long pt = sm.pen[i];
-      float ba = __int_as_float(0x7f800000);
-      long long bl = 0, balt = kInf;
-      int bs = -1;
-      int32_t bg = -1;   // global id of the best source, computed only on a tie of (a32, L(u))
-      const int r0 = sm.rs[i], r1 = sm.rs[i + 1];
-      for (int k = r0; k < r1; ++k) {
-        const int s = sm.anb[k];
-        const long long lu = sm.lab[s];
-        if (lu >= B) continue;                      // not a source of this window (or none)
-        const float c = sm.acost[k];
-        if (!(c < __int_as_float(0x7f800000))) continue;   // blocked arc
-        long long ct;
-        if (!f32_ticks(c, ct)) {
-          bad = true;
-          sm.flag = 0;
-          continue;
-        }
-        const long long alt = lu + ct + pt;
-        if (alt >= kInf) {
-          bad = true;
-          sm.flag = 0;
-          continue;
-        }
-        const float a32 = ticks_f32(alt);
-        int32_t ug = -1;
-        bool take;
-        if (bs < 0 || a32 != ba) {
-          take = a32 < ba;
-        } else if (lu != bl) {
-          take = lu < bl;
-        } else {
-          ug = slot_gid(sm, s);
-          if (bg < 0) bg = slot_gid(sm, bs);
-          take = ug < bg;
-        }
-        if (take) {
-          ba = a32;
-          bl = lu;
-          balt = alt;
-          bs = s;
-          bg = ug;   // -1 unless just computed
-        }
-      }
-      const long long nl = bs >= 0 ? balt : kInf;
-      const int32_t np = bs >= 0 ? (bg >= 0 ? bg : slot_gid(sm, bs)) : -1;
-      if (nl != li || np != sm.par[i]) {
-        atomicOr(&sm.chg[i >> 5], 1u << (i & 31));
-        sm.par[i] = np;
-        if (nl != li) {
-          sm.lab[i] = nl;
-          atomicOr(&sm.lchg[i >> 5], 1u << (i & 31));
-          changed = true;
+    unsigned nev = 0;
+    for (int base = 0; base < nt; base += kT) {
+      const int i = base + tid;
+      bool ch = false, lch = false;
+      if (i < nt) {
+        const long long li = sm.lab[i];
+        bool act = li >= wstart && i != sm.srcl;    // settled nodes and the source never change
+        const int r0 = sm.rs[i], r1 = sm.rs[i + 1];
+        if (act && it > 0) {
+          act = false;
           for (int k = r0; k < r1; ++k) {
             const int s = sm.anb[k];
-            if (s < nt) atomicOr(&sm.wl[cur ^ 1][s >> 5], 1u << (s & 31));
+            if (s < nt && ((sm.wl[prev][s >> 5] >> (s & 31)) & 1u)) {
+              act = true;
+              break;
+            }
+          }
+        }
+        if (act) {
+          ++nev;
+          const long long pt = sm.pen[i];
+          // pass 1: the least alt (ticks); float32 rounding is monotone, so
+          // the winners of (float32(alt), L(u), u) are the candidates whose
+          // alt rounds like it: alt <= hi, the largest such tick count
+          long long amin = kInf;
+          for (int k = r0; k < r1; ++k) {
+            const long long lu = sm.lab[sm.anb[k]];
+            if (lu >= B) continue;                      // not a source of this window (or none)
+            const float c = sm.acost[k];
+            if (!(c < __int_as_float(0x7f800000))) continue;   // blocked arc
+            long long ct;
+            if (!f32_ticks(c, ct)) {
+              bad = true;
+              continue;
+            }
+            const long long alt = lu + ct + pt;
+            if (alt >= kInf) {
+              bad = true;
+              continue;
+            }
+            amin = alt < amin ? alt : amin;
+          }
+          long long nl = kInf;
+          int32_t np = -1;
+          if (amin < kInf) {
+            const long long hi = round_hi(amin);
+            // pass 2: the least (L(u), u) among them
+            long long bl = kInf;
+            int bs = -1;
+            int32_t bg = -1;   // global id of the best source, computed only on a tie of L(u)
+            for (int k = r0; k < r1; ++k) {
+              const int s = sm.anb[k];
+              const long long lu = sm.lab[s];
+              if (lu >= B || lu > bl) continue;
+              const float c = sm.acost[k];
+              if (!(c < __int_as_float(0x7f800000))) continue;
+              long long ct;
+              f32_ticks(c, ct);
+              const long long alt = lu + ct + pt;
+              if (alt > hi) continue;
+              if (lu < bl) {
+                bl = lu;
+                bs = s;
+                nl = alt;
+                bg = -1;
+              } else {                                  // same L(u): the lower node id
+                const int32_t ug = slot_gid(sm, s);
+                if (bg < 0) bg = slot_gid(sm, bs);
+                if (ug < bg) {
+                  bs = s;
+                  nl = alt;
+                  bg = ug;
+                }
+              }
+            }
+            np = bg >= 0 ? bg : slot_gid(sm, bs);
+          }
+          if (nl != li || np != sm.par[i]) {
+            ch = true;
+            sm.par[i] = np;
+            if (nl != li) {
+              sm.lab[i] = nl;
+              lch = true;
+            }
           }
         }
       }
-    });
+      const unsigned bl_ = __ballot_sync(0xffffffffu, lch);
+      const unsigned bc_ = __ballot_sync(0xffffffffu, ch);
+      const int word = (base >> 5) + wid;
+      if (lane == 0 && word < nwords) {
+        sm.wl[cur][word] = bl_;
+        sm.chg[word] |= bc_;
+        sm.lchg[word] |= bl_;
+      }
+      changed |= lch;
+    }
+    if (bad) sm.flag = 0;
+    nev_all += nev;
     // sm.flag is 1 here unless a thread met an arc off the exact grid
     const bool any = __syncthreads_or(changed || bad) != 0;
+    if (it == 0 && tid == 0) atomicAdd(&ogr_tile::g_tile_prof[16], gtimer() - tm0);
     if (any && sm.flag == 0) {
       if (tid == 0) fail(w.ctl, kWhyArcCost);
       return false;
     }
-    for (int k = tid; k < nwords; k += kT) sm.wl[cur][k] = 0u;
-    cur ^= 1;
+    cur = prev;
     if (!any) break;
-    __syncthreads();
   }
+  nev_all = __reduce_add_sync(0xffffffffu, nev_all);
+  if (lane == 0 && nev_all) atomicAdd(&ogr_tile::g_tile_prof[15], (unsigned long long)nev_all);
   if (tid == 0) {
     atomicAdd(&ogr_tile::g_tile_prof[6], (unsigned long long)(it + 1));
     atomicAdd(&ogr_tile::g_tile_prof[7], 1ull);
+    const unsigned long long t1 = gtimer();
+    atomicAdd(&ogr_tile::g_tile_prof[10], t1 - tm0);
+    tm0 = t1;
   }
   // write back; list the tiles beside changed boundary cells; minima
   unsigned long long mn = ~0ull, smn[4] = {~0ull, ~0ull, ~0ull, ~0ull};
@@ -563,7 +640,6 @@ __device__ bool process_tile(Sm& sm, const Geo& G, int t, const ogr_graph& g, co
     }
     if (li >= B && li < kInf) mn = min(mn, (unsigned long long)li);
   });
-  const int lane = tid & 31, wid = tid >> 5;
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
     mn = min(mn, __shfl_xor_sync(0xffffffffu, mn, o));
@@ -596,6 +672,7 @@ __device__ bool process_tile(Sm& sm, const Geo& G, int t, const ogr_graph& g, co
     }
   }
   __syncthreads();
+  if (tid == 0) atomicAdd(&ogr_tile::g_tile_prof[11], gtimer() - tm0);
   return true;
 }
 
@@ -754,9 +831,11 @@ tile_sssp_kernel(ogr_graph g, ogr_state st, ogr_full::Job job, TWs w, Geo G, lon
       const int rcur = rounds % 3, rnext = (rounds + 1) % 3, rclear = (rounds + 2) % 3;
       if (leader) ctl->nlist[rclear] = 0;
       const uint32_t gnext = gr + 1;
+      int nproc = 0;
       if (nlist < 0) {
         for (int t = (int)cta; t < G.ntiles; t += (int)ncta) {
           if (!((abits[t >> 5] >> (t & 31)) & 1u)) continue;
+          ++nproc;
           if (!process_tile(sm, G, t, g, st, a, w, stamp, src, wstart, B, rnext, gnext, wb)) break;
         }
       } else {
@@ -776,11 +855,17 @@ tile_sssp_kernel(ogr_graph g, ogr_state st, ogr_full::Job job, TWs w, Geo G, lon
         if (nown > kMaxOwn) {
           if (tid == 0) fail(ctl, kWhyOwn);
         } else {
+          nproc = nown;
           for (int j = 0; j < nown; ++j)
             if (!process_tile(sm, G, sm.own[j], g, st, a, w, stamp, src, wstart, B, rnext, gnext, wb)) break;
         }
       }
+      const unsigned long long tb0 = tid == 0 ? gtimer() : 0;
       alive = tbarrier(ctl, bar_target, sm);
+      if (tid == 0) {
+        atomicAdd(&ogr_tile::g_tile_prof[12], gtimer() - tb0);
+        atomicMax(&ogr_tile::g_tile_prof[14], (unsigned long long)nproc);
+      }
       ++gr;
       if (!alive) break;
       if (__ldcg(&ctl->err)) {
@@ -952,11 +1037,12 @@ extern "C" int ogr_full_tile(int32_t enable, double delta, int32_t tx, int32_t t
   return OGR_OK;
 }
 
-extern "C" int ogr_tile_profile(int64_t* out8, int32_t reset) {
+extern "C" int ogr_tile_profile(int64_t* out24, int32_t reset) {
+  int64_t* out8 = out24;
   if (!out8) return OGR_ERR_ARG;
-  OGR_CUDA_TRY(cudaMemcpyFromSymbol(out8, ogr_tile::g_tile_prof, sizeof(unsigned long long) * 8));
+  OGR_CUDA_TRY(cudaMemcpyFromSymbol(out8, ogr_tile::g_tile_prof, sizeof(unsigned long long) * 24));
   if (reset) {
-    unsigned long long z[8] = {};
+    unsigned long long z[24] = {};
     OGR_CUDA_TRY(cudaMemcpyToSymbol(ogr_tile::g_tile_prof, z, sizeof(z)));
   }
   return OGR_OK;

@@ -26,7 +26,7 @@ def pstate(s, N, rng, net_id):
 def tile_profile(reset=0):
     import ctypes as C
     from orthoroute_gb300 import _lib
-    out = (C.c_int64 * 8)()
+    out = (C.c_int64 * 24)()
     _lib.check(_lib.load().ogr_tile_profile(out, int(reset)), "ogr_tile_profile")
     return list(out)
 
