@@ -36,22 +36,22 @@ CONFIGS = {
     # the CPU-runnable case: 100x100x6, 200 two-pin nets on layer 0, length 5-80, 10 iterations
     "c0": dict(nx=100, ny=100, nz=6, nets=200, iters=10, seed=1234, clusters=False, plain_iters=None),
     # the headline case: 600x400x12, 2,000 nets, 30% from two 20x20 clusters, <= 40 iterations
-    # plain_iters: the plain one-net-per-launch form is compared on the first iteration only
-    # searches_per_job: searches of the (bit-identical) job, used to scale the CPU sample
+    # plain_iters: the plain one-net-per-launch form is compared with the batched form on the
+    # job's first iterations (all nets, same search engine)
     "c1": dict(nx=600, ny=400, nz=12, nets=2000, iters=40, seed=4321, clusters=True, via_span=4,
-               plain_iters=1, plain_nets=200, searches_per_job=10364,
+               plain_iters=3,
                # DRAM bytes / algorithmic bytes of full_sssp_kernel, ncu on a 300x200x8 search
                traffic_ratio=0.6655),
     # multi-pin batching: 600x400x12, 1,500 multi-pin nets (2-16 pins, 1 + geometric(0.35)) with
     # pins inside a seeded 50x50 box per net, as star two-pin requests p0 -> pi (multipin.py)
     "c2": dict(nx=600, ny=400, nz=12, nets=1500, iters=40, seed=2468, multipin=True, via_span=4,
-               plain_iters=1, plain_nets=300, searches_per_job=52476),
+               plain_iters=3),
     # BGA escape + backplane: 1000x800x32 (25.6 M nodes; 32 layers allow adjacent vias only), a 40x40
     # BGA at 1 mm (2.5 cells) in the centre and four edge-connector rows; reconciled to 1,600 BGA
     # escape nets (ball -> seeded-random connector pin) + 3,200 backplane nets pairing the other
     # 6,400 connector pins, every pin used once (bga_requests); iterations capped for a run
     "c3": dict(nx=1000, ny=800, nz=32, nets=4800, iters=2, seed=1357, bga=True,
-               plain_iters=None, searches_per_job=None),
+               plain_iters=None),
 }
 
 
@@ -164,6 +164,37 @@ def bga_requests(nx, ny, seed, balls=40, pitch_cells=2.5):
     return out
 
 
+def workload_config(name, cfg):
+    """The workload as both arms print it."""
+    return {"workload": name, "lattice": [cfg["nx"], cfg["ny"], cfg["nz"]], "nets": cfg["nets"],
+            "max_iterations": cfg["iters"]}
+
+
+def trajectory_fixture(name):
+    """The oracle's committed trajectory of a workload (per-iteration path
+    fingerprints, searches, wall time of the CPU run), or None."""
+    path = os.path.join(ROOT, "tests", "golden", f"{name}_trajectory.json.gz")
+    if not os.path.exists(path):
+        return None
+    from orthoroute_gb300.trajectory import load
+    return load(path)
+
+
+def host_cpu():
+    """Model and online cores of the host CPU."""
+    model = None
+    try:
+        r = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10)
+        for ln in r.stdout.splitlines():
+            if ln.split(":")[0].strip() in ("Model name", "Model"):
+                model = ln.split(":", 1)[1].strip()
+                if ln.startswith("Model name"):
+                    break
+    except Exception:
+        pass
+    return {"model": model, "nproc": os.cpu_count()}
+
+
 def board_bounds(nx, ny, pitch=0.4):
     sx = (nx - 1) * pitch - 6.0 + 1e-6
     sy = (ny - 1) * pitch - 6.0 + 1e-6
@@ -252,8 +283,22 @@ def run_ours(args, cfg, rank, world):
     router = PathFinderRouter(PathFinderConfig(max_iterations=cfg["iters"]), mode=args.mode,
                               full_engine=args.full_engine)
     router.initialize_lattice(make_lattice(cfg), bounds)
-    for _ in range(args.warmup):
-        job(router)
+    parity = None
+    for w in range(args.warmup):
+        fixture = trajectory_fixture(args.config) if w == 0 else None
+        if fixture is not None:
+            # the first warm-up job is fingerprinted (untimed) against the oracle's run
+            from orthoroute_gb300.trajectory import TrajectoryRecorder, first_difference
+            router.trace = TrajectoryRecorder()
+            job(router)
+            diff = first_difference(router.trace.records, fixture["records"])
+            parity = {"oracle_trajectory": f"tests/golden/{args.config}_trajectory.json.gz",
+                      "iterations_compared": len(fixture["records"]),
+                      "paths_match_every_iteration": diff is None,
+                      "first_difference": None if diff is None else {"record": diff[0], "nets": diff[1]}}
+            router.trace = None
+        else:
+            job(router)
     dist = world > 1
     if dist:
         import torch.distributed as tdist
@@ -290,11 +335,12 @@ def run_ours(args, cfg, rank, world):
         del r2
     plain = None
     if args.mode == "persistent" and args.compare_plain:
-        # plain form: one launch per net, one CTA per search (full-graph nets included), host
-        # round trip per net; compared on the whole job, or on its first iterations for c1
+        # plain form: one launch per net with a host round trip per net, the same search engine
+        # and tuning as the batched form; compared on the whole job, or on its first
+        # iterations (all nets) for the large boards
         k_it = cfg.get("plain_iters") or cfg["iters"]
-        preqs = reqs[:cfg["plain_nets"]] if cfg.get("plain_nets") else reqs
-        whole = k_it == cfg["iters"] and len(preqs) == len(reqs)
+        preqs = reqs
+        whole = k_it == cfg["iters"]
 
         def timed(r, iters):
             r.config = PathFinderConfig(max_iterations=iters)
@@ -305,7 +351,7 @@ def run_ours(args, cfg, rank, world):
             torch.cuda.synchronize()
             return time.perf_counter() - t, out
 
-        rp = PathFinderRouter(PathFinderConfig(max_iterations=k_it), mode="plain", full_engine="cta")
+        rp = PathFinderRouter(PathFinderConfig(max_iterations=k_it), mode="plain", full_engine=args.full_engine)
         rp.initialize_lattice(make_lattice(cfg), bounds)
         t_plain, resp = timed(rp, k_it)
         del rp
@@ -314,7 +360,9 @@ def run_ours(args, cfg, rank, world):
         else:
             t_batched, resb = timed(router, k_it)
         same = {k: list(v) for k, v in resp["paths"].items()} == {k: list(v) for k, v in resb["paths"].items()}
-        plain = {"iterations": k_it, "nets": len(preqs), "plain_s": round(t_plain, 4), "identical_paths": bool(same)}
+        plain = {"iterations": k_it, "nets": len(preqs), "plain_s": round(t_plain, 4), "identical_paths": bool(same),
+                 "engine": "same as the batched form (" + str(router.full_engine) +
+                           (", tile windows" if getattr(router, "full_tile_delta", 0) else "") + ")"}
         if t_batched is not None:
             plain["batched_s"] = round(t_batched, 4)
     ms = max(dev_ms, wall * 1e3) / args.steps
@@ -335,10 +383,10 @@ def run_ours(args, cfg, rank, world):
         "higher_is_better": False, "scaling": "weak" if world > 1 else "weak",
         "vs_baseline": None, "dtype": "f32 costs / f64 labels / int32 indices",
         "data": "synthetic seeded board (seeded nets of the named workload; no dataset)",
-        "config": {"workload": args.config, "lattice": [nx, ny, nz], "nets": cfg["nets"],
-                   "max_iterations": cfg["iters"], "arcs": router.E, "nodes": router.N,
-                   "replicas": "independent per rank" if world > 1 else "single",
-                   "l2": "working set per search < L2; no flush (searches are latency-bound)"},
+        "config": workload_config(args.config, cfg),
+        "workload_info": {"arcs": router.E, "nodes": router.N,
+                          "replicas": "independent per rank" if world > 1 else "single",
+                          "l2": "working set per search < L2; no flush (searches are latency-bound)"},
         "result": {k: res.get(k) for k in ("success", "converged", "iterations", "overuse_sum", "barrel_conflicts",
                                            "failed_nets")},
         "sssp_gteps": round(gteps, 4),
@@ -371,6 +419,8 @@ def run_ours(args, cfg, rank, world):
                                     "ms_per_search": router.tuning.ms_per_search,
                                     "cached": router.tuning.cached})},
     }
+    if parity is not None:
+        line["parity"] = parity
     if plain is not None:
         if "batched_s" not in plain:
             plain["batched_s"] = round(ms / 1e3, 4)
@@ -380,51 +430,126 @@ def run_ours(args, cfg, rank, world):
 
 
 # ---------------------------------------------------------------- CPU baseline
-def cpu_job_sample(cfg, budget_s=20.0, searches_hint=None):
-    """Time the oracle (C heap Dijkstra core) on the job: full job when it
-    fits the budget, else the first iterations, scaled by searches."""
-    from oracle.lattice import LatticeSpec
-    from oracle.loop import Config, OracleRouter
-    reqs = make_requests(cfg)
-    tasks = {n: (s, d) for n, s, d in reqs}
-    nx, ny, nz = cfg["nx"], cfg["ny"], cfg["nz"]
-    t0 = time.perf_counter()
-    R = OracleRouter(LatticeSpec(nx, ny, nz, allowed_via_spans=via_spans(cfg)), board_bounds(nx, ny),
-                     Config(max_iterations=cfg["iters"]), fast=True)
-    if cfg["nets"] <= 400:
-        res = R.route(tasks)
-        dt = time.perf_counter() - t0
-        return dt, f"full job ({res['iterations']} iterations, {R.stats['searches']} searches)", 1
-    # large boards: one routing iteration over a fixed prefix of the nets, timed per search,
-    # scaled by the searches of the whole (bit-identical) job; the policy's own host time is
-    # not added, so the estimate is low
-    sample = dict(list(tasks.items())[:max(4, int(budget_s // 4))])
-    R.cfg.max_iterations = 1
-    t1 = time.perf_counter()
-    R.route(sample)
-    dt = time.perf_counter() - t1
-    per = dt / max(1, R.stats["searches"])
-    n = cfg["searches_per_job"] or searches_hint
-    how = "searches per job"
-    if not n:   # no measured count: one search per net and iteration (an estimate)
-        n, how = len(tasks) * cfg["iters"], "searches per job (estimated: nets x iterations)"
-    return per * n, (f"{R.stats['searches']} searches of iteration 1 ({len(sample)} nets, {dt:.1f} s, "
-                     f"{per:.3f} s/search) x {n} {how}; host policy time excluded"), 1
+class CpuSample:
+    """The CPU restatement of the reference's routing path (the oracle with its
+    C heap Dijkstra), timed on this host's cores on a bounded, stratified
+    sample of a workload.
+
+    Boards of up to 400 nets route the whole job.  Larger boards: the first
+    step routes one stratified chunk of nets through a whole negotiation
+    iteration (the host policy's time per iteration is that step's time minus
+    its searches); every later step routes the next chunk through the
+    routing pass alone (rip-up, search, commit), timing searches.  The job
+    time is the time per search x the searches of the whole job plus the
+    policy time x its iterations, both counts taken from the oracle's own
+    run of the same job (its committed trajectory) when there is one."""
+
+    def __init__(self, name, cfg, chunk=3):
+        from oracle.lattice import LatticeSpec
+        from oracle.loop import Config, OracleRouter
+        self.name, self.cfg = name, cfg
+        reqs = make_requests(cfg)
+        self.tasks = {n: (a, b) for n, a, b in reqs if a != b}
+        nx, ny, nz = cfg["nx"], cfg["ny"], cfg["nz"]
+        self.small = cfg["nets"] <= 400
+        self.R = OracleRouter(LatticeSpec(nx, ny, nz, allowed_via_spans=via_spans(cfg)), board_bounds(nx, ny),
+                              Config(max_iterations=cfg["iters"] if self.small else 1), fast=True)
+        find = self.R._find
+        self.search_s = 0.0
+
+        def timed_find(*a, **k):
+            t = time.perf_counter()
+            try:
+                return find(*a, **k)
+            finally:
+                self.search_s += time.perf_counter() - t
+        self.R._find = timed_find
+        # stratified order: every net of the name order, interleaved from evenly spaced starts
+        names = list(self.tasks)
+        stride = 40
+        self.order = [names[i] for off in range(stride) for i in range(off, len(names), stride)]
+        self.chunk = chunk
+        self.pos = 0
+        self.policy_s = None
+        self.timed_searches = 0
+        self.timed_search_s = 0.0
+        self.full_job_s = None
+
+    def step(self):
+        if self.small:
+            self.R = self.R.__class__(self.R.spec, self.R.bounds, self.R.cfg.__class__(max_iterations=self.cfg["iters"]),
+                                      fast=True)
+            t = time.perf_counter()
+            res = self.R.route(self.tasks)
+            self.full_job_s = time.perf_counter() - t
+            self.small_desc = f"full job ({res['iterations']} iterations, {self.R.stats['searches']} searches)"
+            return
+        sub_names = self.order[self.pos:self.pos + self.chunk]
+        self.pos = (self.pos + self.chunk) % max(1, len(self.order))
+        sub = {n: self.tasks[n] for n in sub_names}
+        s0, n0 = self.search_s, self.R.stats["searches"]
+        t = time.perf_counter()
+        if self.policy_s is None:
+            self.R.route(sub)                                  # one whole iteration
+            self.policy_s = (time.perf_counter() - t) - (self.search_s - s0)
+        else:
+            self.R._route_all(sub, self.tasks)                 # the routing pass alone
+        self.timed_searches += self.R.stats["searches"] - n0
+        self.timed_search_s += self.search_s - s0
+
+    def estimate(self, gpu_counts=None):
+        """(s per job, description)."""
+        if self.small:
+            return self.full_job_s, self.small_desc
+        fx = trajectory_fixture(self.name)
+        if fx is not None:
+            searches, iters = fx["searches"], fx["result"]["iterations"]
+            src = f"the oracle's own run of the job: {searches} searches, {iters} iterations"
+        elif gpu_counts:
+            searches, iters = gpu_counts
+            src = f"this GPU run of the bit-identical job: {searches} searches, {iters} iterations"
+        else:
+            searches, iters = len(self.tasks) * self.cfg["iters"], self.cfg["iters"]
+            src = "no measured count: nets x iterations searches (an estimate)"
+        per = self.timed_search_s / max(1, self.timed_searches)
+        v = per * searches + (self.policy_s or 0.0) * iters
+        return v, (f"stratified sample of iteration 1: {self.timed_searches} searches ({per:.3f} s each) and one "
+                   f"iteration's host policy ({self.policy_s:.1f} s), scaled by {src}")
+
+
+def cpu_job_sample(name, cfg, steps=8, gpu_counts=None):
+    cs = CpuSample(name, cfg)
+    for _ in range(1 if cs.small else steps):
+        cs.step()
+    v, desc = cs.estimate(gpu_counts)
+    return v, desc, 1
 
 
 def run_reference(args, cfg):
-    vals = []
+    """The reference arm: the oracle (the CPU restatement of the reference's
+    routing path, pinned to its own runs) on this host's cores.  Warm-up
+    steps route chunks untimed; each timed step is one more stratified chunk
+    (see CpuSample)."""
+    cs = CpuSample(args.config, cfg)
+    t_steps = []
     for i in range(args.warmup + args.steps):
-        v, sample, cores = cpu_job_sample(cfg)
+        t = time.perf_counter()
+        cs.step()
         if i >= args.warmup:
-            vals.append(v)
-    v = float(np.median(vals))
+            t_steps.append(time.perf_counter() - t)
+        if cs.small and i >= args.warmup:
+            break
+    v, desc = cs.estimate()
+    fx = trajectory_fixture(args.config)
+    cpu = {"value": round(v, 4), "unit": "s/job", "cores": 1, "kind": "port", "sample": desc,
+           "host_cpu": host_cpu()}
+    if fx is not None and fx.get("wall_s"):
+        cpu["full_job_measured_on_build_host_s"] = fx["wall_s"]
     return {"metric": "PathFinder time-to-zero-overuse (s per routing job; capped iterations when not converged)",
             "value": round(v, 4), "unit": "s/job", "impl": "reference", "n_gpus": 1, "steps": args.steps,
             "warmup": args.warmup, "higher_is_better": False,
-            "config": {"workload": args.config, "lattice": [cfg["nx"], cfg["ny"], cfg["nz"]], "nets": cfg["nets"],
-                       "max_iterations": cfg["iters"]},
-            "cpu_baseline": {"value": round(v, 4), "unit": "s/job", "cores": 1, "kind": "port", "sample": sample},
+            "config": workload_config(args.config, cfg),
+            "cpu_baseline": cpu,
             "e2e": {"value": round(v, 4), "unit": "s/job", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
@@ -499,9 +624,13 @@ def main():
         tdist.init_process_group("nccl")
     line = run_ours(args, cfg, rank, world)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        v, sample, cores = cpu_job_sample(cfg, searches_hint=line["searches_per_job"])
+        v, sample, cores = cpu_job_sample(args.config, cfg,
+                                          gpu_counts=(line["searches_per_job"], line["result"]["iterations"]))
         line["cpu_baseline"] = {"value": round(v, 4), "unit": "s/job", "cores": cores, "kind": "port",
-                                "sample": sample}
+                                "sample": sample, "host_cpu": host_cpu()}
+        fx = trajectory_fixture(args.config)
+        if fx is not None and fx.get("wall_s"):
+            line["cpu_baseline"]["full_job_measured_on_build_host_s"] = fx["wall_s"]
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

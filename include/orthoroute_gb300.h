@@ -453,6 +453,19 @@ int ogr_search_lanes(int32_t lanes, int32_t* current);
  * counterpart. */
 int ogr_window_lookahead(int32_t nets, int32_t* current);
 
+/* Limits for tests of failure handling in the phase-settled whole-lattice
+ * search: barrier_spin = n > 0 lets a CTA poll the grid barrier n - 1 times
+ * before it gives up (the search then returns OGR_ERR_TIMEOUT), 0 restores
+ * the default bound; max_phases > 0 caps the settle phases (OGR_ERR_ITER_CAP
+ * when a search needs more), 0 restores the default (2N + 4, never reached);
+ * -1 leaves a setting.  *cur_spin / *cur_phases (host, may be NULL) receive
+ * the settings.  Both failures are ordinary bounded exits: the kernel
+ * returns, the context stays usable, and the routing pass stops before
+ * committing the failed net, so the congestion state matches the stored
+ * paths.  Process-wide; no reference counterpart (the reference raises on a
+ * full queue, pathfinder/persistent_kernel.py:699-700). */
+int ogr_debug_limits(int32_t barrier_spin, int32_t max_phases, int32_t* cur_spin, int32_t* cur_phases);
+
 /* Tracing of the whole-lattice search (host int64[8], cumulative since the
  * last reset): searches, phases, kernel ns, init ns, E-step work ns and
  * S-step work ns of the busiest CTA, barrier wait ns and statistics +
@@ -474,8 +487,11 @@ int ogr_search_profile(int64_t* out16, int32_t reset);
  * node for OGR_NOALLOC_MAX_NODES nodes plus a 16 MB local adjacency, resident on each GPU that loads the library
  * until exit), so lattices above OGR_NOALLOC_MAX_NODES nodes are refused with
  * OGR_ERR_CAPACITY.  The first call on a device looks up that array's device
- * address; make it before any stream capture.  Calls share the array: do not
- * let two calls overlap on the GPU.  Synchronises like ogr_find_path. */
+ * address and keeps it for the process; make it before any stream capture,
+ * and do not call this entry point again after resetting that device
+ * (cudaDeviceReset ends the context that address belongs to).  Calls share
+ * the array: do not let two calls overlap on the GPU.  Synchronises like
+ * ogr_find_path. */
 #define OGR_NOALLOC_MAX_NODES 262144
 int ogr_find_path_noalloc(const ogr_graph* g, const ogr_state* st, const ogr_net_args* net,
                           int32_t* path_out, int32_t path_cap, int32_t* path_len_out,

@@ -6,6 +6,7 @@ routing entry points raise.
 """
 from __future__ import annotations
 
+import contextlib
 import ctypes as C
 import os
 
@@ -31,7 +32,7 @@ EXPORTED = [
     "ogr_window_workspace_bytes", "ogr_window_workspace_init", "ogr_window_ctl_bytes",
     "ogr_multi_workspace_bytes", "ogr_find_path_multi", "ogr_full_grid", "ogr_search_lanes",
     "ogr_paths_commit", "ogr_full_lanes", "ogr_full_reuse", "ogr_window_lookahead",
-    "ogr_full_tile", "ogr_tile_profile",
+    "ogr_full_tile", "ogr_tile_profile", "ogr_debug_limits",
 ]
 
 P = C.c_void_p
@@ -150,6 +151,7 @@ def load(build_if_missing: bool = True):
         "ogr_full_profile": [P, I32],
         "ogr_full_tile": [I32, C.c_double, I32, I32, C.POINTER(I32), C.POINTER(C.c_double)],
         "ogr_tile_profile": [P, I32],
+        "ogr_debug_limits": [I32, I32, C.POINTER(I32), C.POINTER(I32)],
         "ogr_reverse_costs": [I64, P, P, P, P],
         "ogr_full_workspace_init": [P, C.c_size_t, I32, I64, P],
         "ogr_find_path_full": [C.POINTER(Graph), C.POINTER(State), C.POINTER(NetArgs), P, C.c_size_t, P, I32,
@@ -163,6 +165,31 @@ def load(build_if_missing: bool = True):
         fn.restype = C.c_size_t if name.endswith("_bytes") else C.c_int
     _LIB = lib
     return lib
+
+
+@contextlib.contextmanager
+def inject_fault(name: str, rc: int):
+    """Test hook for failure handling: inside the block, calls of the entry
+    point `name` return the status `rc` without running (a stand-in for a
+    device or driver failure reported by that call)."""
+    lib = load()
+    real = getattr(lib, name)
+
+    def fake(*_args, **_kw):
+        return rc
+    setattr(lib, name, fake)
+    try:
+        yield
+    finally:
+        setattr(lib, name, real)
+
+
+def debug_limits(barrier_spin: int = -1, max_phases: int = -1):
+    """Set (>= 0) or read (-1) the whole-lattice search's failure-test limits
+    (ogr_debug_limits): (barrier spin, phase cap), 0 = default."""
+    a, b = C.c_int32(0), C.c_int32(0)
+    check(load().ogr_debug_limits(int(barrier_spin), int(max_phases), C.byref(a), C.byref(b)), "ogr_debug_limits")
+    return int(a.value), int(b.value)
 
 
 def check(rc: int, what: str) -> int:

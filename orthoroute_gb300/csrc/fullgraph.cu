@@ -45,6 +45,11 @@ int g_full_lanes = 16;
 int g_full_reuse = 0;
 constexpr int kStage = 2048;               // staged list entries per CTA and list
 constexpr unsigned kBarSpin = 1u << 22;
+// Limits for tests of failure handling (ogr_debug_limits): the grid
+// barrier's spin bound and a cap on settle phases; the defaults are
+// kBarSpin and 2N + 4 (no search needs more).
+unsigned g_dbg_spin = kBarSpin;
+int g_dbg_phases = 0;
 
 
 struct FCtl {
@@ -78,6 +83,8 @@ struct FWs {
   int32_t* dirty;            // phase in which the node must pull again (an in-neighbour settled)
   float* tcin;               // cin of a carried node's last pull
   int32_t reuse;             // 1: carried nodes with no newly settled in-neighbour skip the pull
+  unsigned bar_spin;         // grid barrier spin bound
+  int32_t max_phases;        // > 0: cap on settle phases (else 2N + 4)
   float* rcost;              // reverse-arc cost gather when the state carries none
   FEntry* fr[3];             // frontier lists: read, write, and the one being cleared
   int32_t* log;              // settled nodes in settle order
@@ -147,7 +154,8 @@ struct Clock {
 // is passed when the counter reaches k * gridDim.x.  The wait is bounded;
 // false when any CTA gave up.  Thread 0 adds the time since the previous
 // barrier to *work and the wait to clk.wait.
-__device__ bool grid_barrier(FCtl* c, unsigned long long& target, Smem& sm, Clock& clk, unsigned long long* work) {
+__device__ bool grid_barrier(FCtl* c, unsigned long long& target, Smem& sm, Clock& clk, unsigned long long* work,
+                             unsigned spin) {
   __syncthreads();
   if (threadIdx.x == 0) {
     const unsigned long long t0 = gtimer();
@@ -158,7 +166,7 @@ __device__ bool grid_barrier(FCtl* c, unsigned long long& target, Smem& sm, Cloc
     asm volatile("red.relaxed.gpu.global.add.u64 [%0], 1;" ::"l"(&c->bar_count) : "memory");
     unsigned it = 0;
     while (ld_acquire_u64(&c->bar_count) < target) {
-      if (++it > kBarSpin || ld_volatile(&c->bar_err)) {
+      if (++it > spin || ld_volatile(&c->bar_err)) {
         atomicExch(&c->bar_err, 1);
         ok = 0;
         break;
@@ -293,8 +301,9 @@ full_sssp_kernel(ogr_graph g, ogr_state st, ogr_full::Job job, FWs w) {
   // (<= gbase) read as unreached / unsettled; when they would run out of range
   // the stamps are cleared (all CTAs read the same persistent word).
   int32_t gbase = __ldcg(&ctl->gbase);
-  const int max_phase = 2 * N + 4;
-  if (gbase < 1 || gbase > 0x7fffffff - (max_phase + 8)) {
+  const int max_phase_natural = 2 * N + 4;
+  const int max_phase = w.max_phases > 0 ? min(w.max_phases, max_phase_natural) : max_phase_natural;
+  if (gbase < 1 || gbase > 0x7fffffff - (max_phase_natural + 8)) {
     for (int64_t r = gtid; r < N; r += gthreads) {
       w.dirty[r] = 0;
       if (r != src) {
@@ -322,7 +331,7 @@ full_sssp_kernel(ogr_graph g, ogr_state st, ogr_full::Job job, FWs w) {
     }
     ctl->nlog = 0;
   }
-  bool alive = grid_barrier(ctl, bar_target, sm, clk, &clk.init);
+  bool alive = grid_barrier(ctl, bar_target, sm, clk, &clk.init, w.bar_spin);
   int status = OGR_OK;
   bool found = false;
   // With statistics requested the search goes on after dst is settled until
@@ -474,7 +483,7 @@ full_sssp_kernel(ogr_graph g, ogr_state st, ogr_full::Job job, FWs w) {
     __syncthreads();
     stage_flush(sm, frn, &ctl->nfront[bn], w.log, &ctl->nlog);
     if (tid == 0 && sm.tmin != ~0ull) atomicMin(&ctl->tbits[bn], sm.tmin);
-    alive = grid_barrier(ctl, bar_target, sm, clk, &clk.e);
+    alive = grid_barrier(ctl, bar_target, sm, clk, &clk.e, w.bar_spin);
     if (!alive) break;
     if (!dst_done) {
       const NodeRec rd = ld_rec(&rec[dst]);
@@ -610,6 +619,8 @@ int launch(const ogr_graph& g, const ogr_state& st, const Job& job, void* ws, cu
   FWs w;
   fws_layout(g.num_nodes, g.num_edges, (char*)ws, &w);
   w.reuse = g_full_reuse;
+  w.bar_spin = g_dbg_spin;
+  w.max_phases = g_dbg_phases;
   ogr_full::Job jv = job;
   jv.gated = 0;
   if (ogr_tile::enabled()) {
@@ -632,6 +643,16 @@ int launch(const ogr_graph& g, const ogr_state& st, const Job& job, void* ws, cu
 }
 
 }  // namespace ogr_full
+
+extern "C" int ogr_debug_limits(int32_t barrier_spin, int32_t max_phases, int32_t* cur_spin,
+                                int32_t* cur_phases) {
+  if (barrier_spin < -1 || max_phases < -1) return OGR_ERR_ARG;
+  if (barrier_spin >= 0) g_dbg_spin = barrier_spin == 0 ? kBarSpin : (unsigned)barrier_spin - 1u;
+  if (max_phases >= 0) g_dbg_phases = max_phases;
+  if (cur_spin) *cur_spin = (int32_t)(g_dbg_spin == kBarSpin ? 0 : g_dbg_spin + 1u);
+  if (cur_phases) *cur_phases = g_dbg_phases;
+  return OGR_OK;
+}
 
 extern "C" int ogr_full_lanes(int32_t lanes, int32_t* current) {
   if (lanes != 0 && lanes != 4 && lanes != 8 && lanes != 16) return OGR_ERR_ARG;

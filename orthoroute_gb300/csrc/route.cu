@@ -35,6 +35,8 @@
 // :7949-8449: rip-up, ROI search, one larger-ROI retry while the pass has
 // fallbacks left, commit) for a whole ordered list of nets in one launch,
 // with every net's current path kept in a device-resident store.
+#include <atomic>
+
 #include "common.cuh"
 #include "fullgraph.cuh"
 
@@ -2013,7 +2015,10 @@ constexpr size_t noalloc_ws_bytes() { return ws_bytes_for((size_t)OGR_NOALLOC_MA
 static __device__ __align__(256) unsigned char g_noalloc_ws[noalloc_ws_bytes()];
 
 constexpr int kMaxDevices = 64;
-void* g_noalloc_ptr[kMaxDevices] = {};
+// Device address of the array per device, looked up on the first call there
+// (atomic: concurrent first calls from several host threads store the same
+// value).  A device reset invalidates it; the process does not reset here.
+std::atomic<void*> g_noalloc_ptr[kMaxDevices] = {};
 
 }  // namespace
 
@@ -2026,15 +2031,15 @@ extern "C" int ogr_find_path_noalloc(const ogr_graph* g, const ogr_state* st, co
   int dev = 0;
   OGR_CUDA_TRY(cudaGetDevice(&dev));
   if (dev < 0 || dev >= kMaxDevices) return OGR_ERR_ARG;
-  if (g_noalloc_ptr[dev] == nullptr) {
-    void* p = nullptr;
-    OGR_CUDA_TRY(cudaGetSymbolAddress(&p, g_noalloc_ws));
-    g_noalloc_ptr[dev] = p;
+  void* base = g_noalloc_ptr[dev].load(std::memory_order_acquire);
+  if (base == nullptr) {
+    OGR_CUDA_TRY(cudaGetSymbolAddress(&base, g_noalloc_ws));
+    g_noalloc_ptr[dev].store(base, std::memory_order_release);
   }
   const size_t need = ws_layout(g->num_nodes, nullptr, nullptr);
   if (need > noalloc_ws_bytes()) return OGR_ERR_CAPACITY;
   Ws w;
-  ws_layout(g->num_nodes, (char*)g_noalloc_ptr[dev], &w);
+  ws_layout(g->num_nodes, (char*)base, &w);
   cudaStream_t s = ogr_stream(stream);
   // The array keeps whatever the previous call left: clear seen[] / g2r[].
   ws_init_kernel<<<ogr_blocks(g->num_nodes, 256), 256, 0, s>>>(w, g->num_nodes);

@@ -33,18 +33,23 @@ def _name_key(name: str):
     return (m.group(1), int(m.group(2)), m.group(3)) if m else (name, -1, "")
 
 
+def _as_i64(path) -> np.ndarray:
+    if isinstance(path, np.ndarray):
+        return path.astype(np.int64, copy=False)
+    return np.fromiter((int(v) for v in (path or ())), dtype=np.int64)
+
+
 def flat_paths(paths: Dict[str, Sequence[int]]) -> np.ndarray:
-    out: List[int] = []
+    parts = []
     for name in sorted(paths, key=_name_key):
-        p = paths[name] or []
-        out.append(len(p))
-        out.extend(int(v) for v in p)
-    return np.asarray(out, dtype=np.int64)
+        p = _as_i64(paths[name])
+        parts.append(np.asarray([len(p)], dtype=np.int64))
+        parts.append(p)
+    return np.concatenate(parts) if parts else np.zeros(0, dtype=np.int64)
 
 
 def path_digest(path: Sequence[int]) -> str:
-    arr = np.asarray(list(path or []), dtype=np.int64)
-    return hashlib.blake2b(arr.tobytes(), digest_size=8).hexdigest()
+    return hashlib.blake2b(_as_i64(path).tobytes(), digest_size=8).hexdigest()
 
 
 class TrajectoryRecorder:

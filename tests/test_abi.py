@@ -52,3 +52,19 @@ def test_edge_count_matches_oracle():
         assert lib.ogr_csr_num_edges(ctypes.byref(d), ctypes.byref(E)) == 0
         ref = build_csr(LatticeSpec(nx, ny, nz, allow_any_layer_via=anyv))
         assert E.value == len(ref.indices)
+
+
+def test_fault_injection_hook_replaces_and_restores_an_entry_point():
+    """The host-side failure hook used by the failure-handling tests: inside
+    the block the entry point returns the injected status without running;
+    afterwards the real entry point is back."""
+    import ctypes as C
+    from orthoroute_gb300 import _lib
+    lib = _lib.load()
+    real = lib.ogr_full_tile
+    cur, d = C.c_int32(0), C.c_double(0.0)
+    with _lib.inject_fault("ogr_full_tile", _lib.OGR_ERR_CUDA):
+        assert lib.ogr_full_tile(-1, 0.0, 0, 0, C.byref(cur), C.byref(d)) == _lib.OGR_ERR_CUDA
+    assert lib.ogr_full_tile is real
+    assert lib.ogr_full_tile(-1, 0.0, 0, 0, C.byref(cur), C.byref(d)) == _lib.OGR_OK
+    assert lib.ogr_debug_limits(-1, -1, None, None) == _lib.OGR_OK
