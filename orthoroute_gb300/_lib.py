@@ -15,7 +15,11 @@ from . import _build
 OGR_OK = 0
 OGR_NO_PATH = 1
 OGR_ERR_ARG = -1
+OGR_ERR_CUDA = -2
 OGR_ERR_CAPACITY = -3
+OGR_ERR_ITER_CAP = -4
+OGR_ERR_NUMERIC = -5
+OGR_ERR_TIMEOUT = -6
 OGR_NOALLOC_MAX_NODES = 262144
 ERRORS = {-1: "bad argument", -2: "CUDA error", -3: "buffer capacity exceeded",
           -4: "device loop iteration limit reached", -5: "exactness precondition violated",
