@@ -131,6 +131,19 @@ int ogr_overused_arcs(int64_t num_edges, const float* present, const float* capa
                       int32_t* out_idx, float* out_val, int32_t out_cap, uint32_t* count,
                       void* stream);
 
+/* Per-net overuse for the negotiation policy's net order, hotset and rip-up
+ * choice (the reference sums max(0, present - capacity) over each net's arcs,
+ * _order_nets_by_difficulty :7840-7901, _rip_top_k_offenders :9751-9781):
+ * for each of num_nets store slots (store_len[k] nodes, arcs at
+ * store_arcs[k * arc_stride], forward then reverse as ogr_route_pass writes
+ * them) sums[k] (double) = the sum over its arcs, hit[k] = 1 if any arc is
+ * overused; canonical_only = 1 counts only arcs with src < dst.  The values
+ * are whole numbers, so the sums are exact.  Asynchronous. */
+int ogr_nets_overuse(const int32_t* store_len, const int32_t* store_arcs, int32_t num_nets,
+                     int64_t arc_stride, const float* present, const float* capacity,
+                     const int32_t* edge_src, const int32_t* indices, int32_t canonical_only,
+                     double* sums, uint8_t* hit, void* stream);
+
 /* ------------------------------------------------------------------ A9 ---
  * Tallies (compute_overuse :1137-1190, _compute_path_node_overuse
  * :10718-10726, _compute_layer_bias's bincount :8473-8500).

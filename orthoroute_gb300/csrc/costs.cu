@@ -264,7 +264,60 @@ __global__ void overused_kernel(int64_t E, const float* __restrict__ present, co
   }
 }
 
+// Per net of a path store: the sum of max(0, present - capacity) over the
+// arcs of its stored path (both directions of every hop) and whether any of
+// them is overused; canonical_only counts only arcs with src < dst.  One warp
+// per net.  The values are whole numbers held exactly in float32, so the
+// double sum is exact in any order.
+__global__ void nets_overuse_kernel(const int32_t* store_len, const int32_t* store_arcs, int32_t num_nets,
+                                    int64_t arc_stride, const float* present, const float* cap,
+                                    const int32_t* edge_src, const int32_t* indices, int32_t canonical_only,
+                                    double* sums, uint8_t* hit) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t n = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; n < num_nets; n += warps) {
+    const int32_t len = store_len[n];
+    const int32_t na = len >= 2 ? 2 * (len - 1) : 0;
+    const int32_t* arcs = store_arcs + n * arc_stride;
+    double sum = 0.0;
+    bool any = false;
+    for (int32_t j = lane; j < na; j += 32) {
+      const int32_t e = arcs[j];
+      if (canonical_only && !(edge_src[e] < indices[e])) continue;
+      const float o = __fsub_rn(present[e], cap[e]);
+      if (o > 0.0f) {
+        sum += (double)o;
+        any = true;
+      }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+    any = __any_sync(0xffffffffu, any);
+    if (lane == 0) {
+      sums[n] = sum;
+      hit[n] = any ? 1 : 0;
+    }
+  }
+}
+
 }  // namespace
+
+extern "C" int ogr_nets_overuse(const int32_t* store_len, const int32_t* store_arcs, int32_t num_nets,
+                                int64_t arc_stride, const float* present, const float* capacity,
+                                const int32_t* edge_src, const int32_t* indices, int32_t canonical_only,
+                                double* sums, uint8_t* hit, void* stream) {
+  if (num_nets < 0 || arc_stride < 0 || (num_nets > 0 && (!store_len || !store_arcs || !present || !capacity ||
+                                                          !sums || !hit)))
+    return OGR_ERR_ARG;
+  if (canonical_only && (!edge_src || !indices)) return OGR_ERR_ARG;
+  if (num_nets == 0) return OGR_OK;
+  const int threads = 256;
+  const int64_t blocks = ((int64_t)num_nets * 32 + threads - 1) / threads;
+  nets_overuse_kernel<<<(int)(blocks < 152 * 16 ? blocks : 152 * 16), threads, 0, ogr_stream(stream)>>>(
+      store_len, store_arcs, num_nets, arc_stride, present, capacity, edge_src, indices, canonical_only, sums, hit);
+  OGR_LAUNCH_CHECK();
+  return OGR_OK;
+}
 
 extern "C" int ogr_via_pools_apply(int64_t E, int32_t nx, int32_t ny, int32_t nz, const int32_t* edge_src,
                                    const int32_t* indices, const uint8_t* edge_kind, const float* col_pres,

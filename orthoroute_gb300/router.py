@@ -305,6 +305,17 @@ class _FlatPaths:
         return self._via
 
 
+class _ArcCount:
+    """Stands for a net's arc list where only its length is kept."""
+    __slots__ = ("size",)
+
+    def __init__(self, n):
+        self.size = int(n)
+
+    def __len__(self):
+        return self.size
+
+
 class _ViaPools:
     """Column / segment via pools on the host (small: Nx*Ny*(Nz-2))."""
 
@@ -638,8 +649,23 @@ class PathFinderRouter:
             raise RuntimeError("overused-arc buffer too small")
         idx = self._ov_idx[:n].cpu().numpy().astype(np.int64)
         val = self._ov_val[:n].cpu().numpy()
+        self.ops.counters["d2h_bytes"] += 4 + 8 * n
         order = np.argsort(idx)
         return idx[order], val[order]
+
+    def _arc_attrs(self, idx):
+        """(src, dst, layer, is_via) of the given arcs, gathered on the device
+        (the policy asks only about its few overused arcs)."""
+        idx = np.asarray(idx, dtype=np.int64)
+        if idx.size == 0:
+            z = np.zeros(0, dtype=np.int64)
+            return z, z, z, np.zeros(0, dtype=bool)
+        g = self.g
+        t = torch.from_numpy(idx).to(g.device)
+        out = [x.index_select(0, t).cpu().numpy() for x in (g.edge_src, g.indices, g.edge_layer, g.edge_kind)]
+        self.ops.counters["h2d_bytes"] += 8 * idx.size
+        self.ops.counters["d2h_bytes"] += 10 * idx.size
+        return (out[0].astype(np.int64), out[1].astype(np.int64), out[2].astype(np.int64), out[3].astype(bool))
 
     def _over_map(self):
         idx, val = self._overused()
@@ -708,8 +734,12 @@ class PathFinderRouter:
         self.s.node_history[d] = torch.from_numpy(self.node_history[nodes]).to(self.g.device)
 
     def _update_tracking(self, name, edges):
+        """Track a committed net's arcs: the arc list itself (plain mode, whose
+        per-net overuse is summed on the host), or only their count (persistent
+        mode sums on the device from the path store)."""
         self.net_to_edges.pop(name, None)
-        self.net_to_edges[name] = np.asarray(edges, dtype=np.int64)
+        self.net_to_edges[name] = (_ArcCount(int(edges)) if isinstance(edges, (int, np.integer))
+                                   else np.asarray(edges, dtype=np.int64))
         self._eidx = None
 
     def _clear_tracking(self, name):
@@ -732,13 +762,15 @@ class PathFinderRouter:
             self._eidx = (names, flat, owner)
         return self._eidx
 
-    def _edge_over(self, over_idx, over_val):
+    def _edge_over(self, over_idx, over_val, canonical_only=False):
         """For every tracked net: (Σ over values of its arcs in its arc order —
         the left-to-right float sum of the reference's generator — and whether
         any of its arcs is in over_idx).  over_idx: sorted arc ids.  The
         overused arcs are looked up through a dense arc-indexed scratch array;
         the result is reused while neither the tracking nor the overuse
         changed (the hotset and the net order of one iteration ask the same)."""
+        if getattr(self, "store", None) is not None:
+            return self._edge_over_device(canonical_only)
         names, flat, owner = self._edge_index()
         k = len(names)
         oi = np.asarray(over_idx, dtype=np.int64)
@@ -768,6 +800,32 @@ class PathFinderRouter:
             out = (names, sums, anyhit)
         self._edge_over_cache = (self._eidx, oi.copy(), ov.copy(), out)
         return out
+
+    def _edge_over_device(self, canonical_only):
+        """The persistent mode's version of _edge_over: every net's overuse sum
+        and hit flag over the arcs of its stored path, computed on the device
+        from the present counts (ogr_nets_overuse) — the same whole-number
+        sums, without the arcs on the host."""
+        st = self.store
+        k = st.num_nets
+        dev = self.g.device
+        if getattr(self, "_nets_over_out", None) is None or self._nets_over_out[0].numel() != k:
+            self._nets_over_out = (torch.empty(k, dtype=torch.float64, device=dev),
+                                   torch.empty(k, dtype=torch.uint8, device=dev))
+        sums, hit = self._nets_over_out
+        g = self.g
+        _lib.check(self.ops.lib.ogr_nets_overuse(
+            st.length.data_ptr(), st.arcs.data_ptr(), k, int(st.arcs.shape[1]), self.s.present.data_ptr(),
+            self.s.capacity.data_ptr(), g.edge_src.data_ptr(), g.indices.data_ptr(), int(bool(canonical_only)),
+            sums.data_ptr(), hit.data_ptr(), self.ops._sp()), "ogr_nets_overuse")
+        lengths = st.length.cpu().numpy()
+        s_h = sums.cpu().numpy()
+        h_h = hit.cpu().numpy().astype(bool)
+        self.ops.counters["launches"] += 1
+        self.ops.counters["d2h_bytes"] += 13 * k
+        rows = np.flatnonzero(lengths >= 2)
+        names = [self._task_names[r] for r in rows.tolist()]
+        return names, s_h[rows], h_h[rows]
 
     # ------------------------------------------------------------- tallies
     def _compute_overuse(self):
@@ -1071,26 +1129,35 @@ class PathFinderRouter:
         self.stats["arcs"] += int(st[0])
         self.stats["pops"] += int(st[1])
         self.full_graph_fallback_count = int(np.count_nonzero(status & 2))
+        # the routed nets' paths, packed on the device to their exact lengths
         lengths = self.store.length.cpu().numpy()
-        idx = torch.as_tensor(order.astype(np.int64), device=self.g.device)
-        L = int(lengths[order].max()) if len(order) else 0
-        rows = torch.index_select(self.store.path[:, :max(L, 1)], 0, idx).cpu().numpy() if len(order) else None
-        arow = (torch.index_select(self.store.arcs[:, :max(2 * (L - 1), 1)], 0, idx).cpu().numpy()
-                if len(order) else None)
-        self.ops.counters["d2h_bytes"] += 4 * lengths.size + (rows.nbytes + arow.nbytes if rows is not None else 0)
+        lens = np.where((status & 1) == 0, lengths[order], 0).astype(np.int64)
+        offs = np.concatenate([[0], np.cumsum(lens)])
+        tot = int(offs[-1])
+        packed = np.zeros(0, dtype=np.int32)
+        if tot:
+            dev = self.g.device
+            rows_d = torch.as_tensor(order.astype(np.int64), device=dev)
+            lens_d = torch.as_tensor(lens, device=dev)
+            rep = torch.repeat_interleave(rows_d, lens_d, output_size=tot)
+            starts = torch.repeat_interleave(torch.as_tensor(offs[:-1], device=dev), lens_d, output_size=tot)
+            pos = torch.arange(tot, device=dev, dtype=torch.int64) - starts
+            flat = rep * self.store.slot_cap + pos
+            packed = self.store.path.view(-1).index_select(0, flat).cpu().numpy()
+            self.ops.counters["h2d_bytes"] += 16 * len(order)
+        self.ops.counters["d2h_bytes"] += 4 * lengths.size + 4 * tot
         paths = self._net_paths
         for k, name in enumerate(ordered):
             old = paths.get(name)
             if old:
                 self._mark_nodes(name, old, -1, paths.array(name))
                 self._clear_tracking(name)
-            n = int(lengths[order[k]])
-            if not (status[k] & 1) and n >= 2:
-                arr = rows[k, :n].astype(np.int64)
-                edges = arow[k, :2 * (n - 1)].astype(np.int64)
+            n = int(lens[k])
+            if n >= 2:
+                arr = packed[offs[k]:offs[k] + n].astype(np.int64)
                 self._mark_nodes(name, None, +1, arr)
                 paths.set_path(name, arr.tolist(), arr)
-                self._update_tracking(name, edges)
+                self._update_tracking(name, 2 * (n - 1))
             else:
                 self.net_paths[name] = []
                 self._clear_tracking(name)
@@ -1316,9 +1383,11 @@ class PathFinderRouter:
 
     def _rip_top_k(self, k=20):
         over_map, over_idx_arr, over_val_arr = self._over_map()
-        keep = np.asarray([self._arc_is_canonical(int(e)) for e in over_idx_arr.tolist()], dtype=bool)
+        a_src, a_dst, _, _ = self._arc_attrs(over_idx_arr)
+        keep = a_src < a_dst                         # canonical arcs (src < dst) only
         enames, esums, ehit = self._edge_over(over_idx_arr[keep] if keep.size else over_idx_arr,
-                                              over_val_arr[keep] if keep.size else over_val_arr)
+                                              over_val_arr[keep] if keep.size else over_val_arr,
+                                              canonical_only=True)
         over_sum_of = {n: float(esums[i]) for i, n in enumerate(enames) if ehit[i]}
         _, _, mscores = self._path_node_conflicts()
         self.path_node_scores = dict(mscores)
@@ -1351,9 +1420,6 @@ class PathFinderRouter:
                 self._clear_tracking(n)
         return victims
 
-    def _arc_is_canonical(self, e):
-        return int(self._edge_src_host[e]) < int(self._indices_host[e])
-
     def _movable_components(self, pairs):
         adj = defaultdict(set)
         for a, b in pairs:
@@ -1373,7 +1439,7 @@ class PathFinderRouter:
     def _layer_congestion(self, idx, val):
         if idx.size == 0:
             return {}
-        lays = self._edge_layer_host[idx]
+        lays = self._arc_attrs(idx)[2]
         out = {}
         for z in range(1, self.nz + 1):
             m = lays == z
@@ -1427,10 +1493,6 @@ class PathFinderRouter:
                 self.store = PathStore(self.g, len(tasks),
                                        window_slots=self.window_slots if self.mode == "persistent" else 0)
             self.store.length.zero_()
-        self._edge_src_host = self.g.edge_src.cpu().numpy()
-        self._indices_host = self.g.indices.cpu().numpy()
-        self._edge_layer_host = self.g.edge_layer.cpu().numpy()
-        self._edge_kind_host = self.g.edge_kind.cpu().numpy().astype(bool)
         self._add_trivial_use()
         return self._negotiate(tasks, progress_cb, iteration_cb)
 
@@ -1516,7 +1578,7 @@ class PathFinderRouter:
                 vmult = float(cfg.via_pressure_multiplier)
             elif pres_fac >= 64:
                 _, idx, val = self._over_map()
-                vo = float(val[self._edge_kind_host[idx]].sum()) if idx.size else 0.0
+                vo = float(val[self._arc_attrs(idx)[3]].sum()) if idx.size else 0.0
                 to = float(val.sum())
                 if to > 0:
                     vmult = 1.5 if vo / to > 0.7 else 0.5
