@@ -124,6 +124,31 @@ int ogr_via_pools_apply(int64_t num_edges, int32_t nx, int32_t ny, int32_t nz,
                         float seg_weight, float pres_fac, int32_t apply_penalty,
                         int32_t apply_block, float* total_cost, void* stream);
 
+/* Via pool use rebuilt from a path store (_rebuild_via_usage_from_committed,
+ * unified_pathfinder.py:4548-4615; per path _accumulate_via_usage_for_path
+ * :4470-4546): every maximal run of via hops in one column adds 1 to the
+ * column and 1 to every segment z - 1 of the run's z hull clamped to
+ * [1, nz-2].  store_len[k] / store_path[k * slot_cap] as ogr_route_pass
+ * keeps them.  scratch: device int32[nx*ny*(1 + max(0, nz-2))].  Writes
+ * col_use[nx][ny] and seg_use[nx][ny][nz-2] (int16, x-major), *spatial
+ * (device int64) = Σ max(0, use - cap) over columns and segments, and the
+ * over-full pools into over[5 * k] = {0 column / 1 segment, x, y, s, use}
+ * with *over_count (device) their number (entries past over_cap are
+ * dropped; call again with more room).  Asynchronous. */
+int ogr_via_pools_rebuild(const int32_t* store_len, const int32_t* store_path, int32_t num_nets,
+                          int64_t slot_cap, int32_t nx, int32_t ny, int32_t nz, int32_t* scratch,
+                          int16_t* col_use, int16_t* seg_use, const int16_t* col_cap,
+                          const int8_t* seg_cap, int64_t* spatial, int32_t* over, int32_t over_cap,
+                          int32_t* over_count, void* stream);
+
+/* The via-present EMA and z prefix (unified_pathfinder.py:6279-6303):
+ * col_pres = 0.6 * max(0, col_use - cap) + 0.4 * col_pres, the same for
+ * seg_pres, seg_prefix = its float32 running sum over z; float32 in numpy's
+ * operation order.  Asynchronous. */
+int ogr_via_pools_presence(int32_t nx, int32_t ny, int32_t nz, const int16_t* col_use,
+                           const int16_t* col_cap, const int16_t* seg_use, const int8_t* seg_cap,
+                           float* col_pres, float* seg_pres, float* seg_prefix, void* stream);
+
 /* Compact the arcs with present > capacity (any order) into out_idx/out_val
  * (max(0,present-cap)); *count (device) receives the total, which may exceed
  * out_cap (then only out_cap entries are written). */

@@ -37,6 +37,7 @@ EXPORTED = [
     "ogr_multi_workspace_bytes", "ogr_find_path_multi", "ogr_full_grid", "ogr_search_lanes",
     "ogr_paths_commit", "ogr_full_lanes", "ogr_full_reuse", "ogr_window_lookahead",
     "ogr_full_tile", "ogr_tile_profile", "ogr_debug_limits", "ogr_nets_overuse",
+    "ogr_via_pools_rebuild", "ogr_via_pools_presence",
 ]
 
 P = C.c_void_p
@@ -157,6 +158,8 @@ def load(build_if_missing: bool = True):
         "ogr_tile_profile": [P, I32],
         "ogr_debug_limits": [I32, I32, C.POINTER(I32), C.POINTER(I32)],
         "ogr_nets_overuse": [P, P, I32, I64, P, P, P, P, I32, P, P, P],
+        "ogr_via_pools_rebuild": [P, P, I32, I64, I32, I32, I32, P, P, P, P, P, P, P, I32, P, P],
+        "ogr_via_pools_presence": [I32, I32, I32, P, P, P, P, P, P, P, P],
         "ogr_reverse_costs": [I64, P, P, P, P],
         "ogr_full_workspace_init": [P, C.c_size_t, I32, I64, P],
         "ogr_find_path_full": [C.POINTER(Graph), C.POINTER(State), C.POINTER(NetArgs), P, C.c_size_t, P, I32,

@@ -300,7 +300,165 @@ __global__ void nets_overuse_kernel(const int32_t* store_len, const int32_t* sto
   }
 }
 
+// Via pool use of the stored paths (_rebuild_via_usage_from_committed,
+// unified_pathfinder.py:4548-4615, per path _accumulate_via_usage_for_path
+// :4470-4546): one thread walks one net's path; every maximal run of via hops
+// in one column adds 1 to that column, and every segment z - 1 of the run's
+// clamped z hull [lo, hi) (z in [1, nz-2]) adds 1 to that segment.  Counts go
+// to int32 scratch ([nx][ny], [nx][ny][segZ], x-major).
+__global__ void via_use_kernel(const int32_t* __restrict__ store_len, const int32_t* __restrict__ store_path,
+                               int32_t num_nets, int64_t slot_cap, int32_t nx, int32_t ny, int32_t nz,
+                               int32_t* col, int32_t* seg) {
+  const int64_t plane = (int64_t)nx * ny;
+  const int segZ = nz > 2 ? nz - 2 : 0;
+  for (int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; n < num_nets;
+       n += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t len = store_len[n];
+    const int32_t* p = store_path + n * slot_cap;
+    int64_t run_xy = -1;
+    int lo = 0, hi = 0;
+    auto close_run = [&]() {
+      if (run_xy >= 0 && segZ > 0)
+        for (int z = lo; z < hi; ++z) {
+          const int sidx = z - 1;
+          if (sidx >= 0 && sidx < segZ) atomicAdd(&seg[run_xy * segZ + sidx], 1);
+        }
+      run_xy = -1;
+    };
+    int32_t u = len > 0 ? p[0] : 0;
+    for (int32_t k = 1; k < len; ++k) {
+      const int32_t v = p[k];
+      const int64_t ru = u % plane, rv = v % plane;
+      const int zu = (int)(u / plane), zv = (int)(v / plane);
+      if (ru == rv && zu != zv) {
+        const int64_t xy = (ru % nx) * ny + ru / nx;
+        int zl = min(zu, zv), zh = max(zu, zv);
+        zl = min(max(zl, 1), nz - 2);
+        zh = min(max(zh, 1), nz - 2);
+        if (xy != run_xy) {
+          close_run();
+          atomicAdd(&col[xy], 1);
+          run_xy = xy;
+          lo = zl;
+          hi = zh;
+        } else {
+          lo = min(lo, zl);
+          hi = max(hi, zh);
+        }
+      } else {
+        close_run();
+      }
+      u = v;
+    }
+    close_run();
+  }
+}
+
+// Per column: the int16 use arrays the penalty / block kernel reads, the
+// spatial overuse sum (Σ max(0, use - cap) over columns and segments) and the
+// list of over-full pools as {kind (0 column, 1 segment), x, y, s, use}.
+__global__ void via_use_finish_kernel(int32_t nx, int32_t ny, int32_t nz, const int32_t* col, const int32_t* seg,
+                                      int16_t* col_use, int16_t* seg_use, const int16_t* col_cap,
+                                      const int8_t* seg_cap, unsigned long long* spatial, int32_t* over,
+                                      int32_t over_cap, int32_t* over_count) {
+  const int64_t plane = (int64_t)nx * ny;
+  const int segZ = nz > 2 ? nz - 2 : 0;
+  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < plane; c += (int64_t)gridDim.x * blockDim.x) {
+    unsigned long long o = 0;
+    const int32_t cu = col[c];
+    col_use[c] = (int16_t)min(cu, 32767);
+    if (cu > col_cap[c]) {
+      o += (unsigned long long)(cu - col_cap[c]);
+      const int k = atomicAdd(over_count, 1);
+      if (k < over_cap) {
+        int32_t* e = over + 5 * (int64_t)k;
+        e[0] = 0; e[1] = (int32_t)(c / ny); e[2] = (int32_t)(c % ny); e[3] = 0; e[4] = cu;
+      }
+    }
+    for (int sidx = 0; sidx < segZ; ++sidx) {
+      const int32_t su = seg[c * segZ + sidx];
+      seg_use[c * segZ + sidx] = (int16_t)min(su, 32767);
+      if (su > seg_cap[c * segZ + sidx]) {
+        o += (unsigned long long)(su - seg_cap[c * segZ + sidx]);
+        const int k = atomicAdd(over_count, 1);
+        if (k < over_cap) {
+          int32_t* e = over + 5 * (int64_t)k;
+          e[0] = 1; e[1] = (int32_t)(c / ny); e[2] = (int32_t)(c % ny); e[3] = sidx; e[4] = su;
+        }
+      }
+    }
+    if (o) atomicAdd(spatial, o);
+  }
+}
+
+// The via-present EMA and z prefix (:6279-6303): pres = 0.6 * over + 0.4 *
+// prev in float32 (numpy's weak-scalar order), prefix = float32 cumulative
+// sum over the column's segments.
+__global__ void via_presence_kernel(int32_t nx, int32_t ny, int32_t nz, const int16_t* col_use,
+                                    const int16_t* col_cap, const int16_t* seg_use, const int8_t* seg_cap,
+                                    float* col_pres, float* seg_pres, float* seg_prefix) {
+  const int64_t plane = (int64_t)nx * ny;
+  const int segZ = nz > 2 ? nz - 2 : 0;
+  const float a = 0.6f, b = 0.4f;
+  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < plane; c += (int64_t)gridDim.x * blockDim.x) {
+    const float oc = (float)max(0, (int)col_use[c] - (int)col_cap[c]);
+    col_pres[c] = __fadd_rn(__fmul_rn(a, oc), __fmul_rn(b, col_pres[c]));
+    float acc = 0.0f;
+    for (int sidx = 0; sidx < segZ; ++sidx) {
+      const int64_t i = c * segZ + sidx;
+      const float os = (float)max(0, (int)seg_use[i] - (int)seg_cap[i]);
+      const float v = __fadd_rn(__fmul_rn(a, os), __fmul_rn(b, seg_pres[i]));
+      seg_pres[i] = v;
+      acc = sidx == 0 ? v : __fadd_rn(acc, v);
+      seg_prefix[i] = acc;
+    }
+  }
+}
+
 }  // namespace
+
+extern "C" int ogr_via_pools_rebuild(const int32_t* store_len, const int32_t* store_path, int32_t num_nets,
+                                     int64_t slot_cap, int32_t nx, int32_t ny, int32_t nz, int32_t* scratch,
+                                     int16_t* col_use, int16_t* seg_use, const int16_t* col_cap,
+                                     const int8_t* seg_cap, int64_t* spatial, int32_t* over, int32_t over_cap,
+                                     int32_t* over_count, void* stream) {
+  if (nx < 1 || ny < 1 || nz < 1 || num_nets < 0 || !scratch || !col_use || !col_cap || !spatial || !over_count)
+    return OGR_ERR_ARG;
+  const int segZ = nz > 2 ? nz - 2 : 0;
+  if (segZ > 0 && (!seg_use || !seg_cap)) return OGR_ERR_ARG;
+  if (num_nets > 0 && (!store_len || !store_path)) return OGR_ERR_ARG;
+  if (over_cap > 0 && !over) return OGR_ERR_ARG;
+  cudaStream_t s = ogr_stream(stream);
+  const int64_t plane = (int64_t)nx * ny;
+  int32_t* col = scratch;
+  int32_t* seg = scratch + plane;
+  OGR_CUDA_TRY(cudaMemsetAsync(scratch, 0, sizeof(int32_t) * (size_t)plane * (1 + segZ), s));
+  OGR_CUDA_TRY(cudaMemsetAsync(spatial, 0, sizeof(int64_t), s));
+  OGR_CUDA_TRY(cudaMemsetAsync(over_count, 0, sizeof(int32_t), s));
+  if (num_nets > 0) {
+    via_use_kernel<<<ogr_blocks(num_nets, 128), 128, 0, s>>>(store_len, store_path, num_nets, slot_cap, nx, ny, nz,
+                                                             col, seg);
+    OGR_LAUNCH_CHECK();
+  }
+  via_use_finish_kernel<<<ogr_blocks(plane, 256), 256, 0, s>>>(
+      nx, ny, nz, col, seg, col_use, seg_use, col_cap, seg_cap, reinterpret_cast<unsigned long long*>(spatial), over,
+      over_cap, over_count);
+  OGR_LAUNCH_CHECK();
+  return OGR_OK;
+}
+
+extern "C" int ogr_via_pools_presence(int32_t nx, int32_t ny, int32_t nz, const int16_t* col_use,
+                                      const int16_t* col_cap, const int16_t* seg_use, const int8_t* seg_cap,
+                                      float* col_pres, float* seg_pres, float* seg_prefix, void* stream) {
+  const int segZ = nz > 2 ? nz - 2 : 0;
+  if (nx < 1 || ny < 1 || !col_use || !col_cap || !col_pres) return OGR_ERR_ARG;
+  if (segZ > 0 && (!seg_use || !seg_cap || !seg_pres || !seg_prefix)) return OGR_ERR_ARG;
+  const int64_t plane = (int64_t)nx * ny;
+  via_presence_kernel<<<ogr_blocks(plane, 256), 256, 0, ogr_stream(stream)>>>(nx, ny, nz, col_use, col_cap, seg_use,
+                                                                            seg_cap, col_pres, seg_pres, seg_prefix);
+  OGR_LAUNCH_CHECK();
+  return OGR_OK;
+}
 
 extern "C" int ogr_nets_overuse(const int32_t* store_len, const int32_t* store_arcs, int32_t num_nets,
                                 int64_t arc_stride, const float* present, const float* capacity,

@@ -326,6 +326,7 @@ class _ViaPools:
         self.col_cap = np.full((nx, ny), col_cap, dtype=np.int16)
         self.col_use = np.zeros((nx, ny), dtype=np.int16)
         self.col_pres = np.zeros((nx, ny), dtype=np.float32)
+        self.device_spatial = None        # set when the use counts come from the device
         if self.has_seg:
             self.seg_cap = np.full((nx, ny, self.segZ), seg_cap, dtype=np.int8)
             self.seg_use = np.zeros((nx, ny, self.segZ), dtype=np.int16)
@@ -368,6 +369,20 @@ class _ViaPools:
         seg = np.bincount(flat_idx, minlength=nx * ny * self.segZ).reshape(nx, ny, self.segZ)
         self.seg_use[:] = seg.astype(np.int16)
 
+    def set_from_device(self, over, spatial):
+        """Host mirror after a device rebuild: use counts of the over-full
+        pools only (rows {kind 0 column / 1 segment, x, y, s, use}; every other
+        pool reads as within capacity) and the spatial overuse sum."""
+        self.col_use[:] = 0
+        if self.has_seg:
+            self.seg_use[:] = 0
+        for kind, x, y, sidx, use in over.tolist():
+            if kind == 0:
+                self.col_use[x, y] = use
+            else:
+                self.seg_use[x, y, sidx] = use
+        self.device_spatial = int(spatial)
+
     def update_presence(self, alpha=0.6, beta=0.4):
         over = np.maximum(0, self.col_use - self.col_cap).astype(np.float32)
         self.col_pres = alpha * over + beta * self.col_pres
@@ -379,6 +394,8 @@ class _ViaPools:
             np.cumsum(self.seg_pres, axis=2, out=self.seg_prefix)
 
     def spatial_overuse(self):
+        if self.device_spatial is not None:
+            return self.device_spatial
         t = int(np.maximum(0, self.col_use - self.col_cap).sum())
         if self.has_seg:
             t += int(np.maximum(0, self.seg_use - self.seg_cap).sum())
@@ -558,6 +575,12 @@ class PathFinderRouter:
             self._d_seg_prefix = torch.zeros((L.nx, L.ny, self.pools.segZ), dtype=torch.float32, device=dev)
             self._d_seg_use = torch.zeros((L.nx, L.ny, self.pools.segZ), dtype=torch.int16, device=dev)
             self._d_seg_cap = torch.from_numpy(self.pools.seg_cap).to(dev)
+            self._d_seg_pres = torch.zeros((L.nx, L.ny, self.pools.segZ), dtype=torch.float32, device=dev)
+        # device via pools (persistent mode): use counts rebuilt from the path store
+        self._d_pool_scratch = torch.zeros(L.nx * L.ny * (1 + self.pools.segZ), dtype=torch.int32, device=dev)
+        self._d_spatial = torch.zeros(1, dtype=torch.int64, device=dev)
+        self._d_pool_over = torch.zeros(5 * 4096, dtype=torch.int32, device=dev)
+        self._d_pool_over_n = torch.zeros(1, dtype=torch.int32, device=dev)
         self._d_disc = torch.zeros(self.nz * self.nz, dtype=torch.float64, device=dev)
         cap = max(1 << 16, min(self.E, 1 << 24))
         self._ov_idx = torch.empty(cap, dtype=torch.int32, device=dev)
@@ -576,6 +599,10 @@ class PathFinderRouter:
         s.layer_bias.fill_(1.0)
         s.use_layer_bias = False
         self.pools = _ViaPools(self.nx, self.ny, self.nz)
+        self._d_col_pres.zero_()
+        if self.pools.has_seg:
+            self._d_seg_pres.zero_()
+            self._d_seg_prefix.zero_()
         self.node_use.fill(0)
         self.node_history.fill(0)
         self._hist_iter = None
@@ -930,20 +957,37 @@ class PathFinderRouter:
         return exact + len(shared)
 
     # ------------------------------------------------------------- device steps
+    def _update_pool_presence(self):
+        """The via-present EMA and z prefix (:6279-6303), on the device arrays
+        in persistent mode."""
+        P = self.pools
+        if P.device_spatial is None:
+            P.update_presence()
+            return
+        seg = P.has_seg
+        _lib.check(self.ops.lib.ogr_via_pools_presence(
+            self.nx, self.ny, self.nz, self._d_col_use.data_ptr(), self._d_col_cap.data_ptr(),
+            self._d_seg_use.data_ptr() if seg else None, self._d_seg_cap.data_ptr() if seg else None,
+            self._d_col_pres.data_ptr(), self._d_seg_pres.data_ptr() if seg else None,
+            self._d_seg_prefix.data_ptr() if seg else None, self.ops._sp()), "ogr_via_pools_presence")
+        self.ops.counters["launches"] += 1
+
     def _upload_pools(self, pres_fac, penalty, block):
         P = self.pools
         dev = self.g.device
-        if penalty:
+        on_device = P.device_spatial is not None        # use / presence already on the device
+        if penalty and not on_device:
             self._d_col_pres.copy_(torch.from_numpy(np.ascontiguousarray(P.col_pres)))
             if P.has_seg:
                 self._d_seg_prefix.copy_(torch.from_numpy(np.ascontiguousarray(P.seg_prefix)))
+        if penalty:
             lb = self.layer_bias
             k = 0.20
             zs = np.arange(self.nz)
             sb = lb[zs]
             disc = (1.0 - k * np.maximum(sb, 0.0))[:, None] * (1.0 + 0.5 * k * np.maximum(lb[zs], 0.0))[None, :]
             self._d_disc.copy_(torch.from_numpy(np.asarray(disc, dtype=np.float64).ravel()))
-        if block:
+        if block and not on_device:
             self._d_col_use.copy_(torch.from_numpy(np.ascontiguousarray(P.col_use)))
             if P.has_seg:
                 self._d_seg_use.copy_(torch.from_numpy(np.ascontiguousarray(P.seg_use)))
@@ -1379,7 +1423,32 @@ class PathFinderRouter:
                        torch.ones(idx.size, dtype=use.dtype, device=use.device))
 
     def _rebuild_via_usage(self):
-        self.pools.rebuild(self._flat())
+        """Column / segment use from the current paths: on the device from the
+        path store in persistent mode (the host keeps only the over-full pools
+        and the spatial overuse sum), else on the host from the flat view."""
+        if getattr(self, "store", None) is None:
+            self.pools.rebuild(self._flat())
+            return
+        P, st = self.pools, self.store
+        seg = P.has_seg
+        while True:
+            cap = int(self._d_pool_over.numel()) // 5
+            _lib.check(self.ops.lib.ogr_via_pools_rebuild(
+                st.length.data_ptr(), st.path.data_ptr(), st.num_nets, st.slot_cap, self.nx, self.ny, self.nz,
+                self._d_pool_scratch.data_ptr(), self._d_col_use.data_ptr(),
+                self._d_seg_use.data_ptr() if seg else None, self._d_col_cap.data_ptr(),
+                self._d_seg_cap.data_ptr() if seg else None, self._d_spatial.data_ptr(),
+                self._d_pool_over.data_ptr(), cap, self._d_pool_over_n.data_ptr(), self.ops._sp()),
+                "ogr_via_pools_rebuild")
+            n = int(self._d_pool_over_n.item())
+            if n <= cap:
+                break
+            self._d_pool_over = torch.zeros(5 * (2 * n), dtype=torch.int32, device=self.g.device)
+        over = self._d_pool_over[:5 * n].view(n, 5).cpu().numpy() if n else np.zeros((0, 5), dtype=np.int32)
+        spatial = int(self._d_spatial.item())
+        self.ops.counters["launches"] += 2
+        self.ops.counters["d2h_bytes"] += 12 + 20 * n
+        P.set_from_device(over, spatial)
 
     def _rip_top_k(self, k=20):
         over_map, over_idx_arr, over_val_arr = self._over_map()
@@ -1568,7 +1637,7 @@ class PathFinderRouter:
             t_it = time.time()
             self._pres_fac_now = pres_fac
             self._rebuild_via_usage()
-            self.pools.update_presence()
+            self._update_pool_presence()
             if it == 1:
                 s.present_ema.copy_(s.present)
             self.ops.present_ema(0.40)

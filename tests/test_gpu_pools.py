@@ -1,0 +1,131 @@
+"""Device via pools and per-net overuse against the oracle on random paths.
+
+* ogr_via_pools_rebuild / ogr_via_pools_presence against oracle.accounting.
+  ViaPools (the restatement of _accumulate_via_usage_for_path :4470-4546 and
+  the EMA / z prefix :6279-6303): column and segment use, the spatial
+  overuse sum, the over-full list, and two EMA steps bit for bit.
+* ogr_nets_overuse against numpy sums over each net's arcs.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+
+def rand_paths(rng, nx, ny, nz, n_paths, max_len):
+    """Paths of lateral and via hops, with via runs up and down a column and
+    columns revisited after a lateral step."""
+    plane = nx * ny
+    out = []
+    for _ in range(n_paths):
+        x, y, z = (int(rng.integers(0, nx)), int(rng.integers(0, ny)), int(rng.integers(0, nz)))
+        p = [z * plane + y * nx + x]
+        for _ in range(int(rng.integers(1, max_len))):
+            r = rng.random()
+            if r < 0.45:
+                z2 = int(rng.integers(0, nz))
+                z = z2 if z2 != z else (z + 1) % nz
+            elif r < 0.7:
+                x = min(nx - 1, max(0, x + int(rng.choice([-1, 1]))))
+            else:
+                y = min(ny - 1, max(0, y + int(rng.choice([-1, 1]))))
+            n = z * plane + y * nx + x
+            if n != p[-1]:
+                p.append(n)
+        out.append(p)
+    return out
+
+
+def store(paths, slot_cap, dev):
+    L = torch.zeros(len(paths), dtype=torch.int32)
+    P = torch.zeros((len(paths), slot_cap), dtype=torch.int32)
+    for k, p in enumerate(paths):
+        L[k] = len(p)
+        P[k, :len(p)] = torch.tensor(p, dtype=torch.int32)
+    return L.to(dev), P.to(dev)
+
+
+@pytest.mark.parametrize("nx,ny,nz,seed", [(12, 9, 8, 1), (20, 16, 12, 2), (7, 5, 3, 3), (16, 12, 2, 4)])
+def test_device_via_pools_match_oracle(nx, ny, nz, seed):
+    from oracle.accounting import ViaPools
+    from orthoroute_gb300 import _lib
+    lib = _lib.load()
+    dev = "cuda"
+    rng = np.random.default_rng(seed)
+    segZ = max(0, nz - 2)
+    ref = ViaPools(nx, ny, nz)
+    col_cap = torch.from_numpy(ref.col_cap).to(dev)
+    seg_cap = torch.from_numpy(ref.seg_cap).to(dev) if segZ else None
+    col_use = torch.zeros((nx, ny), dtype=torch.int16, device=dev)
+    seg_use = torch.zeros((nx, ny, max(segZ, 1)), dtype=torch.int16, device=dev)
+    col_pres = torch.zeros((nx, ny), dtype=torch.float32, device=dev)
+    seg_pres = torch.zeros((nx, ny, max(segZ, 1)), dtype=torch.float32, device=dev)
+    seg_prefix = torch.zeros_like(seg_pres)
+    scratch = torch.zeros(nx * ny * (1 + segZ), dtype=torch.int32, device=dev)
+    spatial = torch.zeros(1, dtype=torch.int64, device=dev)
+    over = torch.zeros(5 * 8192, dtype=torch.int32, device=dev)
+    over_n = torch.zeros(1, dtype=torch.int32, device=dev)
+    for step in range(2):
+        paths = rand_paths(rng, nx, ny, nz, 60, 40)
+        L, P = store(paths, 64, dev)
+        rc = lib.ogr_via_pools_rebuild(L.data_ptr(), P.data_ptr(), len(paths), 64, nx, ny, nz, scratch.data_ptr(),
+                                       col_use.data_ptr(), seg_use.data_ptr() if segZ else None, col_cap.data_ptr(),
+                                       seg_cap.data_ptr() if segZ else None, spatial.data_ptr(), over.data_ptr(),
+                                       8192, over_n.data_ptr(), None)
+        assert rc == _lib.OGR_OK
+        rc = lib.ogr_via_pools_presence(nx, ny, nz, col_use.data_ptr(), col_cap.data_ptr(),
+                                        seg_use.data_ptr() if segZ else None, seg_cap.data_ptr() if segZ else None,
+                                        col_pres.data_ptr(), seg_pres.data_ptr() if segZ else None,
+                                        seg_prefix.data_ptr() if segZ else None, None)
+        assert rc == _lib.OGR_OK
+        ref.rebuild(paths)
+        ref.update_presence()
+        np.testing.assert_array_equal(col_use.cpu().numpy(), ref.col_use)
+        assert int(spatial.item()) == ref.spatial_overuse_total()
+        n = int(over_n.item())
+        got = {tuple(r) for r in over[:5 * n].view(n, 5).cpu().numpy().tolist()}
+        want = {(0, x, y, 0, int(ref.col_use[x, y])) for x, y in zip(*np.nonzero(ref.col_use > ref.col_cap))}
+        np.testing.assert_array_equal(col_pres.cpu().numpy(), ref.col_pres)
+        if segZ:
+            np.testing.assert_array_equal(seg_use.cpu().numpy(), ref.seg_use)
+            want |= {(1, x, y, s, int(ref.seg_use[x, y, s]))
+                     for x, y, s in zip(*np.nonzero(ref.seg_use > ref.seg_cap))}
+            np.testing.assert_array_equal(seg_pres.cpu().numpy(), ref.seg_pres)
+            np.testing.assert_array_equal(seg_prefix.cpu().numpy(), ref.seg_prefix)
+        assert got == want, step
+
+
+@pytest.mark.parametrize("canonical", [0, 1])
+def test_nets_overuse_matches_numpy(canonical):
+    from orthoroute_gb300 import _lib
+    lib = _lib.load()
+    dev = "cuda"
+    rng = np.random.default_rng(7 + canonical)
+    E, K, cap = 5000, 300, 40
+    present = rng.integers(0, 4, size=E).astype(np.float32)
+    capacity = np.ones(E, dtype=np.float32)
+    src = rng.integers(0, 900, size=E).astype(np.int32)
+    dst = rng.integers(0, 900, size=E).astype(np.int32)
+    lens = rng.integers(0, cap // 2 + 1, size=K).astype(np.int32)
+    arcs = np.zeros((K, cap), dtype=np.int32)
+    for k in range(K):
+        na = 2 * (lens[k] - 1) if lens[k] >= 2 else 0
+        arcs[k, :na] = rng.integers(0, E, size=na)
+    t = lambda a: torch.from_numpy(a).to(dev)
+    sums = torch.zeros(K, dtype=torch.float64, device=dev)
+    hit = torch.zeros(K, dtype=torch.uint8, device=dev)
+    rc = lib.ogr_nets_overuse(t(lens).data_ptr(), t(arcs).data_ptr(), K, cap, t(present).data_ptr(),
+                              t(capacity).data_ptr(), t(src).data_ptr(), t(dst).data_ptr(), canonical,
+                              sums.data_ptr(), hit.data_ptr(), None)
+    assert rc == _lib.OGR_OK
+    over = np.maximum(0, present - capacity).astype(np.float64)
+    for k in range(K):
+        na = 2 * (lens[k] - 1) if lens[k] >= 2 else 0
+        a = arcs[k, :na]
+        if canonical:
+            a = a[src[a] < dst[a]]
+        assert sums[k].item() == over[a].sum()
+        assert bool(hit[k].item()) == bool((over[a] > 0).any())
