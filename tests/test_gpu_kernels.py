@@ -428,15 +428,21 @@ def test_autotune_times_every_candidate(tmp_path, monkeypatch):
     try:
         t = autotune.tune(ops, lat, nets)
         assert not t.cached and t.samples == 2
+        # the tile engine's window widths are timed when the grid engine wins
+        tile = {f"tile_delta{h}" for h in autotune.TILE_DELTA_HOPS} if t.full_engine == "grid" else set()
         assert set(t.ms_per_search) == ({f"grid{c}" for _, c in autotune.candidates(lim)[:-1]} | {"cta"} |
-                                        {f"full_lanes{k}_reuse{r}" for k in autotune.FULL_LANES for r in (0, 1)})
+                                        {f"full_lanes{k}_reuse{r}" for k in autotune.FULL_LANES for r in (0, 1)} |
+                                        tile)
         assert autotune.full_lanes(0) == t.full_lanes and autotune.full_reuse() == t.full_reuse
         assert t.full_engine in ("grid", "cta")
         if t.full_engine == "grid":
             assert autotune.full_grid(0)[0] == t.full_ctas
+        assert autotune.full_tile(-1) == ((1, t.full_tile_delta) if t.full_tile_delta > 0 else (0, autotune.full_tile(-1)[1]))
         t2 = autotune.tune(ops, lat, nets)
-        assert t2.cached and (t2.full_engine, t2.full_ctas) == (t.full_engine, t.full_ctas)
+        assert t2.cached and (t2.full_engine, t2.full_ctas, t2.full_tile_delta) == \
+            (t.full_engine, t.full_ctas, t.full_tile_delta)
     finally:
+        autotune.full_tile(0)
         autotune.full_grid(cur)
         autotune.full_lanes(16)
         autotune.full_reuse(0)

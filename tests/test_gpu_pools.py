@@ -114,13 +114,16 @@ def test_nets_overuse_matches_numpy(canonical):
     for k in range(K):
         na = 2 * (lens[k] - 1) if lens[k] >= 2 else 0
         arcs[k, :na] = rng.integers(0, E, size=na)
-    t = lambda a: torch.from_numpy(a).to(dev)
+    # the device copies must outlive the asynchronous launch: keep them named
+    d = {k: torch.from_numpy(v).to(dev) for k, v in dict(lens=lens, arcs=arcs, present=present, capacity=capacity,
+                                                          src=src, dst=dst).items()}
     sums = torch.zeros(K, dtype=torch.float64, device=dev)
     hit = torch.zeros(K, dtype=torch.uint8, device=dev)
-    rc = lib.ogr_nets_overuse(t(lens).data_ptr(), t(arcs).data_ptr(), K, cap, t(present).data_ptr(),
-                              t(capacity).data_ptr(), t(src).data_ptr(), t(dst).data_ptr(), canonical,
+    rc = lib.ogr_nets_overuse(d["lens"].data_ptr(), d["arcs"].data_ptr(), K, cap, d["present"].data_ptr(),
+                              d["capacity"].data_ptr(), d["src"].data_ptr(), d["dst"].data_ptr(), canonical,
                               sums.data_ptr(), hit.data_ptr(), None)
     assert rc == _lib.OGR_OK
+    torch.cuda.synchronize()
     over = np.maximum(0, present - capacity).astype(np.float64)
     for k in range(K):
         na = 2 * (lens[k] - 1) if lens[k] >= 2 else 0
