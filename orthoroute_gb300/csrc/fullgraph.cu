@@ -344,7 +344,22 @@ full_sssp_kernel(ogr_graph g, ogr_state st, ogr_full::Job job, FWs w) {
   while (alive) {
     const int b = phase % 3, bn = (phase + 1) % 3, bz = (phase + 2) % 3;
     const int32_t gp = gbase + 1 + phase;
+    // the frontier length, T and (until it settles) dst's record, issued as
+    // one batch of loads after the barrier
     const int nf = __ldcg(&ctl->nfront[b]);
+    const unsigned long long tb = __ldcg(&ctl->tbits[b]);
+    if (!dst_done && phase > 0) {
+      const NodeRec rd = ld_rec(&rec[dst]);
+      if (rd.sp > gbase) {
+        dst_done = true;
+        ld = rd.lab;
+        if (!want_stats) {
+          found = true;
+          --phase;             // no work of this phase was done
+          break;
+        }
+      }
+    }
     if (nf == 0) {
       if (dst_done)
         found = true;
@@ -352,7 +367,7 @@ full_sssp_kernel(ogr_graph g, ogr_state st, ogr_full::Job job, FWs w) {
         status = OGR_NO_PATH;
       break;
     }
-    const double T = __longlong_as_double((long long)__ldcg(&ctl->tbits[b]));
+    const double T = __longlong_as_double((long long)tb);
     if (dst_done && T > ld) {
       found = true;
       break;
@@ -485,17 +500,6 @@ full_sssp_kernel(ogr_graph g, ogr_state st, ogr_full::Job job, FWs w) {
     if (tid == 0 && sm.tmin != ~0ull) atomicMin(&ctl->tbits[bn], sm.tmin);
     alive = grid_barrier(ctl, bar_target, sm, clk, &clk.e, w.bar_spin);
     if (!alive) break;
-    if (!dst_done) {
-      const NodeRec rd = ld_rec(&rec[dst]);
-      if (rd.sp > gbase) {
-        dst_done = true;
-        ld = rd.lab;
-        if (!want_stats) {
-          found = true;
-          break;
-        }
-      }
-    }
     if (++phase > max_phase) {
       status = OGR_ERR_ITER_CAP;
       break;
