@@ -435,20 +435,21 @@ int ogr_find_path_full(const ogr_graph* g, const ogr_state* st, const ogr_net_ar
  * results do not depend on it): ctas > 0 sets the number of cooperative CTAs
  * (at most *limit = SMs x resident CTAs per SM), 0 only reads.  *current and
  * *limit (host, may be NULL) receive the grid in use and the maximum.  The
- * setting is per device and process-wide.  Chosen by the autotuner
+ * setting is per device and per host thread.  Chosen by the autotuner
  * (orthoroute_gb300/autotune.py); no reference counterpart. */
 int ogr_full_grid(int32_t ctas, int32_t* current, int32_t* limit);
 
 /* Lanes per examined frontier node of the whole-lattice search (4, 8 or 16;
  * default 16) for searches launched afterwards; 0 only reads.  A tuning
- * knob (results do not depend on it), process-wide, chosen by the
+ * knob (results do not depend on it), per host thread (each job of a
+ * server routes in its own thread), chosen by the
  * autotuner; no reference counterpart. */
 int ogr_full_lanes(int32_t lanes, int32_t* current);
 
 /* Whether the whole-lattice search keeps the last pull of a carried frontier
  * node none of whose in-neighbours settled since (mode 1) or pulls every
  * frontier node every phase (0, default); -1 only reads.  A tuning knob
- * (results do not depend on it), process-wide, chosen by the autotuner; no
+ * (results do not depend on it), per host thread, chosen by the autotuner; no
  * reference counterpart. */
 int ogr_full_reuse(int32_t mode, int32_t* current);
 
@@ -461,7 +462,7 @@ int ogr_full_reuse(int32_t mode, int32_t* current);
  * grid step; a net it cannot take (a cost or penalty below 2^-7, a label
  * of 2^23 or more, a tile over capacity, an iteration cap) is searched by
  * the phase engine in the same stream, so results, statistics and status
- * codes do not depend on this setting.  Process-wide, chosen by the
+ * codes do not depend on this setting.  Per host thread, chosen by the
  * autotuner; the window width is the delta of a delta-stepping search; no
  * reference counterpart. */
 int ogr_full_tile(int32_t enable, double delta, int32_t tx, int32_t ty, int32_t* cur_enable,
@@ -479,7 +480,7 @@ int ogr_tile_profile(int64_t* out24, int32_t reset);
 /* Lanes per node of the single-CTA ROI search (2, 4, 8 or 16; default 4) for
  * every search launched afterwards; 0 only reads.  *current (host, may be
  * NULL) receives the setting.  A tuning knob (results do not depend on it),
- * process-wide, chosen by the autotuner; no reference counterpart. */
+ * per host thread, chosen by the autotuner; no reference counterpart. */
 int ogr_search_lanes(int32_t lanes, int32_t* current);
 
 /* How many clashing nets a disjoint-ROI window of ogr_route_pass may skip
@@ -487,7 +488,7 @@ int ogr_search_lanes(int32_t lanes, int32_t* current);
  * reads.  A later net joins only if its footprint also misses every skipped
  * net's footprint grown to its fallback ROI bound, and a member that fails
  * while nets before it are pending is undone and retried in its turn, so
- * results equal the sequential pass.  Process-wide; no reference
+ * results equal the sequential pass.  Per host thread; no reference
  * counterpart. */
 int ogr_window_lookahead(int32_t nets, int32_t* current);
 
@@ -500,7 +501,7 @@ int ogr_window_lookahead(int32_t nets, int32_t* current);
  * the settings.  Both failures are ordinary bounded exits: the kernel
  * returns, the context stays usable, and the routing pass stops before
  * committing the failed net, so the congestion state matches the stored
- * paths.  Process-wide; no reference counterpart (the reference raises on a
+ * paths.  Per host thread; no reference counterpart (the reference raises on a
  * full queue, pathfinder/persistent_kernel.py:699-700). */
 int ogr_debug_limits(int32_t barrier_spin, int32_t max_phases, int32_t* cur_spin, int32_t* cur_phases);
 

@@ -28,6 +28,8 @@
 // clears per-node memory.  List appends are staged per CTA in shared memory.
 #include <cooperative_groups.h>
 
+#include <atomic>
+
 #include "fullgraph.cuh"
 
 namespace cg = cooperative_groups;
@@ -35,21 +37,23 @@ namespace cg = cooperative_groups;
 namespace {
 
 constexpr int kThreads = 512;
+// The tuning knobs below are per host thread: each job of a server routes in
+// its own thread and keeps its own settings.
 // Lanes per examined frontier node: 4, 8 or 16 (one instantiation each,
 // chosen at launch by ogr_full_lanes; results do not depend on it).  Narrow
 // groups keep more nodes in flight when rows are short and fronts are wide.
-int g_full_lanes = 16;
+thread_local int g_full_lanes = 16;
 // Reuse of clean carried nodes' last pull (ogr_full_reuse): it saves the
 // pulls of wide fronts of waiting nodes and costs a stamp load per entry and
 // state stores per carried node; which wins depends on the lattice.
-int g_full_reuse = 0;
+thread_local int g_full_reuse = 0;
 constexpr int kStage = 2048;               // staged list entries per CTA and list
 constexpr unsigned kBarSpin = 1u << 22;
 // Limits for tests of failure handling (ogr_debug_limits): the grid
 // barrier's spin bound and a cap on settle phases; the defaults are
 // kBarSpin and 2N + 4 (no search needs more).
-unsigned g_dbg_spin = kBarSpin;
-int g_dbg_phases = 0;
+thread_local unsigned g_dbg_spin = kBarSpin;
+thread_local int g_dbg_phases = 0;
 
 
 struct FCtl {
@@ -579,8 +583,8 @@ full_sssp_kernel(ogr_graph g, ogr_state st, ogr_full::Job job, FWs w) {
 }
 
 constexpr int kMaxDevices = 64;
-int g_grid_blocks[kMaxDevices] = {};   // grid of the cooperative launch (0: not sized yet)
-int g_grid_limit[kMaxDevices] = {};    // SMs x resident CTAs per SM
+thread_local int g_grid_blocks[kMaxDevices] = {};   // grid of the cooperative launch (0: not sized yet)
+std::atomic<int> g_grid_limit[kMaxDevices] = {};    // SMs x resident CTAs per SM (a device property)
 
 int size_grid(int dev) {
   if (g_grid_limit[dev] == 0) {

@@ -54,11 +54,11 @@ constexpr int kSearchLanes = OGR_SEARCH_LANES;  // default lanes per node of the
 // Lanes per node of the ROI search for the launches that follow (set by
 // ogr_search_lanes; the autotuner picks it per lattice).  Every searching
 // kernel exists for 2, 4, 8 and 16 lanes; results do not depend on the choice.
-int g_search_lanes = kSearchLanes;
+thread_local int g_search_lanes = kSearchLanes;
 
 // Nets a disjoint-ROI window may skip over to take later disjoint ones
 // (ogr_window_lookahead; 0 = consecutive nets only).
-int g_window_look = 8;
+thread_local int g_window_look = 8;
 
 #define OGR_WITH_LANES(LV, ...)                                \
   do {                                                         \

@@ -41,6 +41,8 @@
 // above the window bound.
 #include <cooperative_groups.h>
 
+#include <atomic>
+
 #include "fullgraph.cuh"
 
 namespace ogr_tile {
@@ -68,11 +70,12 @@ constexpr unsigned long long kTickMask = (1ULL << 53) - 1;
 constexpr int kStampMax = 2047;                  // 11-bit search stamp, 0 = never valid
 constexpr unsigned kBarSpin = 1u << 22;
 
-// Knobs of the engine (ogr_full_tile): tile size in cells and the window
-// width delta in label units; enable = 0 keeps the phase engine.
-int g_tile_enable = 0;
-int g_tile_tx = 0, g_tile_ty = 0;                 // 0: chosen from the lattice
-double g_tile_delta = 0.0;
+// Knobs of the engine (ogr_full_tile), per host thread: tile size in cells
+// and the window width delta in label units; enable = 0 keeps the phase
+// engine.
+thread_local int g_tile_enable = 0;
+thread_local int g_tile_tx = 0, g_tile_ty = 0;    // 0: chosen from the lattice
+thread_local double g_tile_delta = 0.0;
 
 struct TCtl {
   alignas(128) unsigned long long bar_count;     // monotone arrival counter (zeroed per launch)
@@ -944,8 +947,8 @@ tile_sssp_kernel(ogr_graph g, ogr_state st, ogr_full::Job job, TWs w, Geo G, lon
 }
 
 constexpr int kMaxDevices = 64;
-int g_tile_grid[kMaxDevices] = {};
-size_t g_tile_smem[kMaxDevices] = {};
+std::atomic<int> g_tile_grid[kMaxDevices] = {};       // device properties, set once
+std::atomic<size_t> g_tile_smem[kMaxDevices] = {};
 
 Geo make_geo(const ogr_graph& g) {
   Geo G{};
@@ -1013,8 +1016,8 @@ int launch(const ogr_graph& g, const ogr_state& st, const ogr_full::Job& job, vo
   ogr_full::Job jv = job;
   Geo gg = G;
   void* args[] = {&gv, &sv, &jv, &w, &gg, &delta, &res, &gate};
-  OGR_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)tile_sssp_kernel, dim3(g_tile_grid[dev]), dim3(kT), args,
-                                           g_tile_smem[dev], s));
+  OGR_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)tile_sssp_kernel, dim3(g_tile_grid[dev].load()), dim3(kT),
+                                           args, g_tile_smem[dev].load(), s));
   return OGR_OK;
 }
 

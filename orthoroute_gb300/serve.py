@@ -7,7 +7,9 @@ job gets a worker thread, its own CUDA stream and its own device-resident
 router state (CSR, congestion arrays, path store and workspaces) for the
 whole job, so jobs overlap on the device: one job's kernels run while
 another job's host policy runs (the ctypes calls release the interpreter
-lock), and single-CTA kernels of different jobs share the SMs.  Every
+lock), single-CTA kernels of different jobs share the SMs, and each job's
+whole-lattice searches use a 1/slots share of the resident CTAs, so the
+cooperative searches of concurrent jobs fit on the GPU together.  Every
 kernel is deterministic, so a job's result is the same alone and in the mix.
 
 The reference has no serving loop; its unit of work is one
@@ -87,8 +89,9 @@ class RouteServer:
 
     def __init__(self, slots: int = 4, hbm_budget_bytes: int = 160 * (1 << 30), device: str = "cuda",
                  window_slots: int = 32, executor: Optional[Callable[[RouteJob], Dict]] = None,
-                 footprint: Optional[Callable[[RouteJob], int]] = None):
+                 footprint: Optional[Callable[[RouteJob], int]] = None, sm_share: bool = True):
         self.slots = max(1, int(slots))
+        self.sm_share = bool(sm_share)
         self.budget = int(hbm_budget_bytes)
         self.device = device
         self.window_slots = int(window_slots)
@@ -186,6 +189,13 @@ class RouteServer:
         from .router import PathFinderConfig, PathFinderRouter
         stream = torch.cuda.Stream(device=self.device)
         with torch.cuda.device(self.device), torch.cuda.stream(stream):
+            if self.sm_share:
+                # this job's whole-lattice searches take a 1/slots share of the
+                # resident CTAs (the grid knob is per host thread), so
+                # cooperative searches of concurrent jobs fit on the GPU together
+                from .autotune import full_grid
+                _, limit = full_grid(0)
+                full_grid(max(1, limit // self.slots))
             r = PathFinderRouter(PathFinderConfig(max_iterations=job.max_iterations), device=self.device,
                                  window_slots=self.window_slots)
             r.initialize_lattice(Lattice(job.nx, job.ny, job.nz, allowed_via_spans=job.allowed_via_spans),

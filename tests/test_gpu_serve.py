@@ -59,3 +59,28 @@ def test_job_writes_its_solution_as_ors(tmp_path):
     assert len(md["iteration_metrics"]) == res.result["iterations"]
     routed = {n for n, p in res.result["paths"].items() if len(p) >= 2}
     assert set(geom["by_net"]) <= routed and geom["all_tracks"]
+
+
+def test_concurrent_whole_lattice_searches_agree():
+    """Two jobs whose nets all need whole-lattice searches (Manhattan length
+    >= 125), each on its share of the resident CTAs, run together: the same
+    paths and tallies as each job alone on the whole GPU."""
+    def jobs():
+        out = []
+        for i in range(2):
+            nets = _nets(170, 40, 14, 30 + i, dmax=200)
+            nets = [(n, s, d) for n, s, d in nets if abs(s % 170 - d % 170) + abs(s // 170 - d // 170) >= 125]
+            out.append(RouteJob(f"W{i}", 170, 40, 6, nets[:6], max_iterations=3, bounds=_bounds(170, 40)))
+        return out
+    js = jobs()
+    assert all(len(j.requests) >= 3 for j in js)
+    alone_srv = RouteServer(slots=1, sm_share=False)
+    alone = [f.result() for f in [alone_srv.submit(j) for j in jobs()]]
+    alone_srv.close()
+    mix_srv = RouteServer(slots=2)
+    mixed = [f.result() for f in [mix_srv.submit(j) for j in jobs()]]
+    mix_srv.close()
+    assert mix_srv.peak_running == 2
+    for a, m in zip(alone, mixed):
+        assert a.error is None and m.error is None, (a.error, m.error)
+        assert a.result == m.result, a.name
