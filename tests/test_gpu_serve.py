@@ -65,15 +65,20 @@ def test_concurrent_whole_lattice_searches_agree():
     """Two jobs whose nets all need whole-lattice searches (Manhattan length
     >= 125), each on its share of the resident CTAs, run together: the same
     paths and tallies as each job alone on the whole GPU."""
-    def jobs():
+    def long_nets(n, seed, nx=170, ny=40):
+        rng = np.random.default_rng(seed)
         out = []
-        for i in range(2):
-            nets = _nets(170, 40, 14, 30 + i, dmax=200)
-            nets = [(n, s, d) for n, s, d in nets if abs(s % 170 - d % 170) + abs(s // 170 - d // 170) >= 125]
-            out.append(RouteJob(f"W{i}", 170, 40, 6, nets[:6], max_iterations=3, bounds=_bounds(170, 40)))
+        for k in range(n):
+            x0, x1 = int(rng.integers(0, 15)), int(rng.integers(nx - 15, nx))
+            y0, y1 = int(rng.integers(0, ny)), int(rng.integers(0, ny))
+            out.append((f"N{k}", y0 * nx + x0, y1 * nx + x1))
         return out
+
+    def jobs():
+        return [RouteJob(f"W{i}", 170, 40, 6, long_nets(6, 30 + i), max_iterations=3, bounds=_bounds(170, 40))
+                for i in range(2)]
     js = jobs()
-    assert all(len(j.requests) >= 3 for j in js)
+    assert all(abs(s % 170 - d % 170) + abs(s // 170 - d // 170) >= 125 for j in js for _, s, d in j.requests)
     alone_srv = RouteServer(slots=1, sm_share=False)
     alone = [f.result() for f in [alone_srv.submit(j) for j in jobs()]]
     alone_srv.close()
