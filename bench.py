@@ -553,6 +553,72 @@ def run_reference(args, cfg):
             "e2e": {"value": round(v, 4), "unit": "s/job", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
+def run_engine_compare(args):
+    """Whole-lattice searches on one lattice with uncongested costs (base 0.12
+    plus the reference's index jitter), timed per engine: the phase-settled
+    search and the tile-window search at several window widths.  The paths
+    must be identical; the line gives ms per search and the engines' own
+    counters (phases / grid rounds, windows, per-stage time)."""
+    import ctypes as C
+    import torch
+    from orthoroute_gb300 import Lattice, _lib, autotune
+    from orthoroute_gb300.device import DeviceGraph, DeviceState, Ops
+    cfg = CONFIGS[args.config]
+    if args.lattice:
+        nx, ny, nz = (int(v) for v in args.lattice.lower().split("x"))
+        lat = Lattice(nx, ny, nz, allowed_via_spans=[(a, b) for a, b in Lattice(2, 2, nz).via_pairs() if b - a <= 4])
+    else:
+        lat = make_lattice(cfg)
+    g = DeviceGraph(lat)
+    s = DeviceState(g)
+    s.enable_rcost()
+    ops = Ops(g, s)
+    jit = (np.arange(g.E) % 9973).astype(np.float32) * np.float32(1e-6)
+    s.total_cost.copy_(torch.from_numpy((np.float32(0.12) + jit).astype(np.float32)))
+    ops.sync_rcost()
+    nx, ny = lat.nx, lat.ny
+    rng = np.random.default_rng(5)
+    pairs = [(5 + (ny // 10) * nx, nx * ny - 7 - (ny // 13) * nx)]
+    pairs += [(int(rng.integers(0, nx * ny)), int(rng.integers(0, nx * ny))) for _ in range(2)]
+
+    def prof(fn, n):
+        out = (C.c_int64 * n)()
+        _lib.check(getattr(_lib.load(), fn)(out, 1), fn)
+        return list(out)
+
+    engines = [("phase", 0.0)] + [(f"tile_delta{d}", d) for d in (0.5, 1.0, 2.0, 4.0)]
+    res = {}
+    paths = {}
+    for name, delta in engines:
+        autotune.full_tile(1 if delta else 0, delta)
+        ops.find_path(ops.net_args(0, pairs[0][0], pairs[0][1], full_graph=True, penalty=False), engine="grid")
+        prof("ogr_full_profile", 8)
+        prof("ogr_tile_profile", 24)
+        torch.cuda.synchronize()
+        t0 = ops.counters["search_ms"]
+        got = [ops.find_path(ops.net_args(0, a, b, full_graph=True, penalty=False), engine="grid") for a, b in pairs]
+        ms = (ops.counters["search_ms"] - t0) / len(pairs)
+        fp, tp = prof("ogr_full_profile", 8), prof("ogr_tile_profile", 24)
+        paths[name] = got
+        r = {"ms_per_search": round(ms, 3)}
+        if delta:
+            r.update(rounds=tp[1] // len(pairs), windows=tp[2] // len(pairs), handed_over=tp[4],
+                     stage_ns_per_cta={"structure": tp[8] // len(pairs), "labels": tp[9] // len(pairs),
+                                       "iterations": tp[10] // len(pairs), "write_back": tp[11] // len(pairs),
+                                       "barrier_wait": tp[12] // len(pairs)},
+                     local_iterations_per_tile=round(tp[6] / max(1, tp[7]), 2), tiles_processed=tp[7] // len(pairs))
+        else:
+            r.update(phases=fp[1] // len(pairs))
+        res[name] = r
+    autotune.full_tile(0)
+    same = all(paths[k] == paths["phase"] for k in paths)
+    return {"metric": "whole-lattice search time by engine (ms per search)", "unit": "ms",
+            "config": {"workload": args.config, "lattice": [lat.nx, lat.ny, lat.nz], "arcs": int(g.E),
+                       "costs": "0.12 + index jitter (uncongested)", "searches": len(pairs),
+                       "path_lengths": [len(p or []) for p in paths["phase"]]},
+            "identical_paths": bool(same), "engines": res}
+
+
 def run_serving(args):
     """A bounded prefix of the serving stream through RouteServer: p50 / p99
     job latency (arrival to completion) and jobs per second."""
@@ -601,6 +667,9 @@ def main():
     ap.add_argument("--mode", default="persistent", choices=["persistent", "plain"])
     ap.add_argument("--full-engine", default="auto", choices=["auto", "grid", "cta"],
                     help="engine of full-graph nets; auto = autotuned per lattice")
+    ap.add_argument("--compare-engines", action="store_true",
+                    help="time the whole-lattice search engines on the workload's lattice and exit")
+    ap.add_argument("--lattice", default=None, help="with --compare-engines: NXxNYxNZ instead of the workload's")
     ap.add_argument("--compare-plain", action="store_true", default=True)
     ap.add_argument("--no-compare-plain", dest="compare_plain", action="store_false")
     args = ap.parse_args()
@@ -609,6 +678,10 @@ def main():
             print(json.dumps(run_serving(args)), flush=True)
         elif args.impl == "reference":
             print(json.dumps({"impl": "reference", "unavailable": "the reference has no serving loop"}), flush=True)
+        return
+    if args.compare_engines:
+        if int(os.environ.get("RANK", "0")) == 0:
+            print(json.dumps(run_engine_compare(args)), flush=True)
         return
     cfg = CONFIGS[args.config]
     if args.steps is None:
