@@ -392,8 +392,15 @@ def run_ours(args, cfg, rank, world):
         "sssp_gteps": round(gteps, 4),
         # device time of the search launches (CUDA events on the routing stream) vs the whole job
         "time_split": {"search_kernels_s": round(search_ms / 1e3 / max(1, args.steps), 3),
+                       # wall time of the routing passes (launch to sync) and everything else: the host
+                       # negotiation policy, tallies, cost updates and their transfers
+                       "routing_passes_s": round(prof["search_wall_s"] / max(1, args.steps), 3),
+                       "host_policy_and_rest_s": round((ms / 1e3) - prof["search_wall_s"] / max(1, args.steps), 3),
                        "job_s": round(ms / 1e3, 3)},
         "searches_per_job": prof["searches"] // max(1, args.steps),
+        # window searches whose results were undone (an earlier member of their window failed);
+        # their nets were searched again and that search is the one counted above
+        "discarded_window_searches_per_job": prof["discarded_searches"] // max(1, args.steps),
         "roofline": {"bound": "hbm", "achieved": round(achieved, 3), "peak": pk.get("hbm_gbs"), "unit": "GB/s",
                      "frac": round(achieved / pk.get("hbm_gbs", 1.0), 6),
                      "traffic": (round(cfg["traffic_ratio"] * alg_bytes / max(1, prof["searches"])) if

@@ -169,6 +169,30 @@ int ogr_nets_overuse(const int32_t* store_len, const int32_t* store_arcs, int32_
                      const int32_t* edge_src, const int32_t* indices, int32_t canonical_only,
                      double* sums, uint8_t* hit, void* stream);
 
+/* Exact barrel conflicts and shared path nodes of the stored paths
+ * (_detect_barrel_conflicts, unified_pathfinder.py:10778-11111, with
+ * _detect_path_node_conflicts :10564-10606), as device lists the host turns
+ * into the conflict sets, pairs and scores.  For every hop (u, v) of the
+ * stored path of slot n (net id net_id[n]) an endpoint conflicts when its
+ * barrel owner (from owner_count / owner_xor: -1 none, the id for one net,
+ * -2 for several) is neither -1 nor the net's id.  counts (device int64[5],
+ * zeroed here) = {conflicting hops, occ entries, cnode entries, member
+ * entries, shared entries}; each list holds min(count, cap) entries:
+ *   occ[2i..]    (endpoint node, net id) of every conflicting endpoint of
+ *                every conflicting hop (two for a hop conflicting at both);
+ *   cnode[3i..]  (node, owner_count, owner_xor) of each distinct conflict node;
+ *   member[2i..] (node, net id) of the nets whose via hops span a conflict
+ *                node that several nets own (repeats possible);
+ *   shared[2i..] (node, slot) of every stored-path node with path-node use
+ *                above 1.
+ * mark: device int32[num_nodes] scratch whose entries differ from `stamp` on
+ * entry (use a new stamp per call).  Asynchronous. */
+int ogr_barrel_scan(const int32_t* store_len, const int32_t* store_path, const int32_t* net_id,
+                    int32_t num_nets, int64_t slot_cap, int32_t nx, int32_t ny,
+                    const int32_t* owner_count, const int32_t* owner_xor, const int32_t* path_node_use,
+                    int32_t* mark, int32_t stamp, int64_t cap, int32_t* occ, int32_t* cnode,
+                    int32_t* member, int32_t* shared, int64_t* counts, void* stream);
+
 /* ------------------------------------------------------------------ A9 ---
  * Tallies (compute_overuse :1137-1190, _compute_path_node_overuse
  * :10718-10726, _compute_layer_bias's bincount :8473-8500).
@@ -290,14 +314,15 @@ int ogr_find_path_multi(const ogr_graph* g, const float* costs, const int32_t* r
  * ownership of every via-spanned node, no live refresh.  Path k is
  * nodes[offsets[k] .. offsets[k+1]) (device int32, >= 2 nodes each) of net
  * net_ids[k]; its arcs (forward then reverse) go to
- * arcs_out[2 * (offsets[k] - k) ..].  With store_path / store_len (may be
- * NULL) the path is also written to slot store_slot[k] of a path store with
- * slot_cap nodes per slot.  The paths must not be committed already; the
+ * arcs_out[2 * (offsets[k] - k) ..].  With store_path / store_len /
+ * store_arcs (each may be NULL) the path, its length and its arcs are also
+ * written to slot store_slot[k] of a path store with slot_cap nodes and
+ * 2 * slot_cap arcs per slot.  The paths must not be committed already; the
  * result equals committing them one by one in any order.  *status_dev:
  * 0, 1 (a hop is not an arc) or 2 (capacity).  Asynchronous. */
 int ogr_paths_commit(const ogr_graph* g, const ogr_state* st, const int32_t* nodes, const int32_t* offsets,
                      const int32_t* net_ids, int32_t n_paths, int32_t* arcs_out, int32_t* store_path,
-                     int32_t* store_len, const int32_t* store_slot, int32_t slot_cap,
+                     int32_t* store_len, int32_t* store_arcs, const int32_t* store_slot, int32_t slot_cap,
                      int32_t* status_dev, void* stream);
 
 /* Commit (sign=+1) or rip up (sign=-1) a path given as device node ids:
@@ -382,13 +407,18 @@ typedef struct {
  * fallback in order.  The results are those of the sequential pass.
  * ws holds `slots` search slots of slot_bytes (ogr_window_workspace_*),
  * scratch holds slots x slot_cap path nodes, ctl is device scratch of
- * ogr_window_ctl_bytes(slots) bytes. */
+ * ogr_window_ctl_bytes(slots) bytes.  discarded (device int64[3], may be
+ * NULL) accumulates {searches, arcs scanned, nodes popped} of the window
+ * searches whose results were undone because an earlier member of their
+ * window failed: those nets are searched again later, and only accepted
+ * searches count in the pass's `stats`. */
 typedef struct {
   int32_t slots;
   size_t slot_bytes;
   void* ws;
   int32_t* scratch;
   void* ctl;
+  int64_t* discarded;
 } ogr_window_args;
 
 size_t ogr_window_workspace_bytes(int32_t num_nodes, int32_t max_roi_nodes, int32_t slots);
@@ -430,6 +460,27 @@ int ogr_full_workspace_init(void* workspace, size_t workspace_bytes, int32_t num
 int ogr_find_path_full(const ogr_graph* g, const ogr_state* st, const ogr_net_args* net,
                        void* workspace, size_t workspace_bytes, int32_t* path_out,
                        int32_t path_cap, int32_t* path_len_out, int64_t* stats, void* stream);
+
+/* Whole-lattice multi-source multi-sink search: the portal-seeded route of a
+ * long net (the reference's full-graph seeded search,
+ * find_path_fullgraph_gpu_seeds, pathfinder/cuda_dijkstra.py:5516, with the
+ * CPU semantics of SimpleDijkstra.find_path_multisource_multisink,
+ * unified_pathfinder.py:2550-2659, on roi_nodes = all nodes).  seeds
+ * (device int32[n_seeds], distinct) start with label seed_cost (device
+ * float64, >= 0) + their node penalty and no parent, ahead of every
+ * relaxation with the same float32 value; targets (device int32[n_targets],
+ * distinct) settle but never expand; the search runs until nothing is left
+ * and returns the path to the target with the least (label + target_cost,
+ * label, node id), seed first.  The node penalty and net id come from `net`
+ * (its src / dst are not used).  A repeated or out-of-range seed or target,
+ * a negative or NaN seed cost or a NaN target cost is OGR_ERR_ARG.
+ * Workspace as ogr_find_path_full.  stats (may be NULL): arcs of the
+ * expanded nodes, nodes settled, lattice size, settle phases.  Synchronises. */
+int ogr_find_path_full_multi(const ogr_graph* g, const ogr_state* st, const ogr_net_args* net,
+                             const int32_t* seeds, const double* seed_cost, int32_t n_seeds,
+                             const int32_t* targets, const double* target_cost, int32_t n_targets,
+                             void* workspace, size_t workspace_bytes, int32_t* path_out, int32_t path_cap,
+                             int32_t* path_len_out, int64_t* stats, void* stream);
 
 /* Grid of the whole-lattice search on the current device (a tuning knob;
  * results do not depend on it): ctas > 0 sets the number of cooperative CTAs

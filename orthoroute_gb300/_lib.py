@@ -37,7 +37,7 @@ EXPORTED = [
     "ogr_multi_workspace_bytes", "ogr_find_path_multi", "ogr_full_grid", "ogr_search_lanes",
     "ogr_paths_commit", "ogr_full_lanes", "ogr_full_reuse", "ogr_window_lookahead",
     "ogr_full_tile", "ogr_tile_profile", "ogr_debug_limits", "ogr_nets_overuse",
-    "ogr_via_pools_rebuild", "ogr_via_pools_presence",
+    "ogr_via_pools_rebuild", "ogr_via_pools_presence", "ogr_barrel_scan", "ogr_find_path_full_multi",
 ]
 
 P = C.c_void_p
@@ -95,7 +95,8 @@ class RoiBatch(C.Structure):
 
 
 class WindowArgs(C.Structure):
-    _fields_ = [("slots", I32), ("slot_bytes", C.c_size_t), ("ws", P), ("scratch", P), ("ctl", P)]
+    _fields_ = [("slots", I32), ("slot_bytes", C.c_size_t), ("ws", P), ("scratch", P), ("ctl", P),
+                ("discarded", P)]
 
 
 _LIB = None
@@ -150,7 +151,7 @@ def load(build_if_missing: bool = True):
         "ogr_full_lanes": [I32, C.POINTER(I32)],
         "ogr_full_reuse": [I32, C.POINTER(I32)],
         "ogr_window_lookahead": [I32, C.POINTER(I32)],
-        "ogr_paths_commit": [C.POINTER(Graph), C.POINTER(State), P, P, P, I32, P, P, P, P, I32, P, P],
+        "ogr_paths_commit": [C.POINTER(Graph), C.POINTER(State), P, P, P, I32, P, P, P, P, P, I32, P, P],
         "ogr_find_path_multi": [C.POINTER(Graph), P, P, I32, P, P, P, I32, P, P, I32, P, C.c_size_t, P, I32,
                                 C.POINTER(I32), P, P],
         "ogr_full_profile": [P, I32],
@@ -160,10 +161,13 @@ def load(build_if_missing: bool = True):
         "ogr_nets_overuse": [P, P, I32, I64, P, P, P, P, I32, P, P, P],
         "ogr_via_pools_rebuild": [P, P, I32, I64, I32, I32, I32, P, P, P, P, P, P, P, I32, P, P],
         "ogr_via_pools_presence": [I32, I32, I32, P, P, P, P, P, P, P, P],
+        "ogr_barrel_scan": [P, P, P, I32, I64, I32, I32, P, P, P, P, I32, I64, P, P, P, P, P, P],
         "ogr_reverse_costs": [I64, P, P, P, P],
         "ogr_full_workspace_init": [P, C.c_size_t, I32, I64, P],
         "ogr_find_path_full": [C.POINTER(Graph), C.POINTER(State), C.POINTER(NetArgs), P, C.c_size_t, P, I32,
                                C.POINTER(I32), P, P],
+        "ogr_find_path_full_multi": [C.POINTER(Graph), C.POINTER(State), C.POINTER(NetArgs), P, P, I32, P, P, I32,
+                                     P, C.c_size_t, P, I32, C.POINTER(I32), P, P],
         "ogr_bfs_workspace_bytes": [I32, I64, I32],
         "ogr_bfs_workspace_init": [P, I32, I64, I32, P],
     }

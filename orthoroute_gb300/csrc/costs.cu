@@ -415,6 +415,101 @@ __global__ void via_presence_kernel(int32_t nx, int32_t ny, int32_t nz, const in
   }
 }
 
+// Barrel owner of a node from the device ownership (count of distinct nets
+// whose via hops span it, XOR of their ids): -1 none, the id, -2 several.
+__device__ __forceinline__ int32_t barrel_owner(const int32_t* cnt, const int32_t* xr, int32_t n) {
+  const int32_t c = cnt[n];
+  return c == 0 ? -1 : (c == 1 ? xr[n] : -2);
+}
+
+// Reserve one slot of list k (counts[k]) and return it, or -1 past the cap
+// (the count still grows, so the host learns the size it needs).
+__device__ __forceinline__ long long list_slot(unsigned long long* counts, int k, long long cap) {
+  const long long i = (long long)atomicAdd(&counts[k], 1ull);
+  return i < cap ? i : -1;
+}
+
+// Exact barrel conflicts and shared path nodes of the stored paths
+// (_detect_barrel_conflicts, unified_pathfinder.py:10778-11111;
+// _detect_path_node_conflicts :10564-10606).  One warp per net, lanes over
+// the path: hop (u, v) of net id en conflicts at an endpoint whose barrel
+// owner is neither -1 nor en.  counts: {conflicting hops, endpoint
+// occurrences, distinct conflict nodes, multi-owner members, shared-node
+// occurrences}.
+__global__ void barrel_hops_kernel(const int32_t* __restrict__ store_len, const int32_t* __restrict__ store_path,
+                                   const int32_t* __restrict__ net_id, int32_t num_nets, int64_t slot_cap,
+                                   const int32_t* __restrict__ owner_count, const int32_t* __restrict__ owner_xor,
+                                   const int32_t* __restrict__ use, int32_t* mark, int32_t stamp, long long cap,
+                                   int32_t* occ, int32_t* cnode, int32_t* shared, unsigned long long* counts) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t n = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; n < num_nets; n += warps) {
+    const int32_t len = store_len[n];
+    if (len < 2) continue;
+    const int32_t* p = store_path + n * slot_cap;
+    const int32_t en = net_id[n];
+    unsigned hops = 0;
+    for (int32_t j = lane; j < len; j += 32) {
+      const int32_t u = p[j];
+      if (use[u] > 1) {
+        const long long i = list_slot(counts, 4, cap);
+        if (i >= 0) { shared[2 * i] = u; shared[2 * i + 1] = (int32_t)n; }
+      }
+      if (j + 1 >= len) continue;
+      const int32_t v = p[j + 1];
+      const int32_t ou = barrel_owner(owner_count, owner_xor, u);
+      const int32_t ov = barrel_owner(owner_count, owner_xor, v);
+      const bool sc = ou != -1 && ou != en;
+      const bool dc = ov != -1 && ov != en;
+      if (!(sc || dc)) continue;
+      ++hops;
+      for (int k = 0; k < 2; ++k) {
+        if (!(k == 0 ? sc : dc)) continue;
+        const int32_t x = k == 0 ? u : v;
+        const long long i = list_slot(counts, 1, cap);
+        if (i >= 0) { occ[2 * i] = x; occ[2 * i + 1] = en; }
+        if (atomicExch(&mark[x], stamp) != stamp) {
+          const long long c = list_slot(counts, 2, cap);
+          if (c >= 0) { cnode[3 * c] = x; cnode[3 * c + 1] = owner_count[x]; cnode[3 * c + 2] = owner_xor[x]; }
+        }
+      }
+    }
+    hops = __reduce_add_sync(0xffffffffu, hops);
+    if (lane == 0 && hops) atomicAdd(&counts[0], (unsigned long long)hops);
+  }
+}
+
+// The nets behind each conflict node that several nets own: every via hop
+// (same column, different layers) spans the nodes of its z range; a spanned
+// node marked in this call whose owner count is 2 or more gets (node, id).
+// A net may list a node twice (two hops over it); the set is what counts.
+__global__ void barrel_members_kernel(const int32_t* __restrict__ store_len, const int32_t* __restrict__ store_path,
+                                      const int32_t* __restrict__ net_id, int32_t num_nets, int64_t slot_cap,
+                                      int32_t plane, const int32_t* __restrict__ owner_count,
+                                      const int32_t* __restrict__ mark, int32_t stamp, long long cap, int32_t* member,
+                                      unsigned long long* counts) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t n = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; n < num_nets; n += warps) {
+    const int32_t len = store_len[n];
+    if (len < 2) continue;
+    const int32_t* p = store_path + n * slot_cap;
+    const int32_t en = net_id[n];
+    for (int32_t j = lane; j + 1 < len; j += 32) {
+      const int32_t u = p[j], v = p[j + 1];
+      const int32_t ru = u % plane, rv = v % plane;
+      const int zu = u / plane, zv = v / plane;
+      if (ru != rv || zu == zv) continue;
+      for (int z = min(zu, zv); z <= max(zu, zv); ++z) {
+        const int32_t nd = z * plane + ru;
+        if (mark[nd] != stamp || owner_count[nd] < 2) continue;
+        const long long i = list_slot(counts, 3, cap);
+        if (i >= 0) { member[2 * i] = nd; member[2 * i + 1] = en; }
+      }
+    }
+  }
+}
+
 }  // namespace
 
 extern "C" int ogr_via_pools_rebuild(const int32_t* store_len, const int32_t* store_path, int32_t num_nets,
@@ -500,6 +595,30 @@ extern "C" int ogr_overused_arcs(int64_t E, const float* present, const float* c
   OGR_CUDA_TRY(cudaMemsetAsync(count, 0, sizeof(uint32_t), s));
   overused_kernel<<<ogr_blocks(E, kThreads, 152 * 32), kThreads, 0, s>>>(E, present, capacity, out_idx, out_val,
                                                                           out_cap, count);
+  OGR_LAUNCH_CHECK();
+  return OGR_OK;
+}
+
+extern "C" int ogr_barrel_scan(const int32_t* store_len, const int32_t* store_path, const int32_t* net_id,
+                               int32_t num_nets, int64_t slot_cap, int32_t nx, int32_t ny,
+                               const int32_t* owner_count, const int32_t* owner_xor, const int32_t* path_node_use,
+                               int32_t* mark, int32_t stamp, int64_t cap, int32_t* occ, int32_t* cnode,
+                               int32_t* member, int32_t* shared, int64_t* counts, void* stream) {
+  if (num_nets < 0 || nx < 1 || ny < 1 || cap < 0 || slot_cap < 2 || !counts) return OGR_ERR_ARG;
+  if (num_nets > 0 && (!store_len || !store_path || !net_id || !owner_count || !owner_xor || !path_node_use ||
+                       !mark || (cap > 0 && (!occ || !cnode || !member || !shared))))
+    return OGR_ERR_ARG;
+  cudaStream_t s = ogr_stream(stream);
+  OGR_CUDA_TRY(cudaMemsetAsync(counts, 0, 5 * sizeof(int64_t), s));
+  if (num_nets == 0) return OGR_OK;
+  unsigned long long* c = reinterpret_cast<unsigned long long*>(counts);
+  const int threads = 256;
+  const int blocks = ogr_blocks((int64_t)num_nets * 32, threads);
+  barrel_hops_kernel<<<blocks, threads, 0, s>>>(store_len, store_path, net_id, num_nets, slot_cap, owner_count,
+                                                owner_xor, path_node_use, mark, stamp, cap, occ, cnode, shared, c);
+  OGR_LAUNCH_CHECK();
+  barrel_members_kernel<<<blocks, threads, 0, s>>>(store_len, store_path, net_id, num_nets, slot_cap, nx * ny,
+                                                   owner_count, mark, stamp, cap, member, c);
   OGR_LAUNCH_CHECK();
   return OGR_OK;
 }

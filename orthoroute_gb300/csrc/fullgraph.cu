@@ -65,7 +65,14 @@ struct FCtl {
   alignas(128) int32_t res[4];
   int32_t gbase;                               // persistent across searches
   int32_t tile_gate;                           // 1: the tile engine handed this net over
+  int32_t merr;                                // multi-source: a bad or repeated seed / target
+  unsigned long long mk[3];                    // multi-source: the chosen target's keys
 };
+
+// Multi-source searches mark seeds and targets in per-node doubles that hold
+// this NaN pattern otherwise (written by the workspace init, restored by
+// every search).
+constexpr unsigned long long kNoTerm = 0x7ff8deadbeef0001ull;
 
 // Per-node search record: label, settle stamp, reach stamp in one 16-byte
 // load.  A reader uses lab only where sp says the node settled in an earlier
@@ -94,6 +101,8 @@ struct FWs {
   int32_t* log;              // settled nodes in settle order
   FCtl* ctl;
   char* tile;                // scratch of the tile-window engine
+  double* mseed;             // multi-source: seed cost per node (kNoTerm bits otherwise)
+  double* mtgt;              // multi-source: target cost per node (kNoTerm bits otherwise)
 };
 
 constexpr size_t r256(size_t v) { return (v + 255) & ~(size_t)255; }
@@ -116,6 +125,8 @@ size_t fws_layout(int32_t N, int64_t E, char* base, FWs* w) {
   for (int i = 0; i < 3; ++i) t.fr[i] = (FEntry*)take(16 * n);
   t.log = (int32_t*)take(4 * n);
   t.tile = take(ogr_tile::workspace_bytes(N));
+  t.mseed = (double*)take(8 * n);
+  t.mtgt = (double*)take(8 * n);
   if (w) *w = t;
   return off;
 }
@@ -239,6 +250,11 @@ __device__ __forceinline__ void stage_reset(Smem& sm) {
   __syncthreads();
 }
 
+// Multi-source: whether node u is marked in a seed / target array.
+__device__ __forceinline__ bool is_term(const double* arr, int32_t u) {
+  return (unsigned long long)__double_as_longlong(__ldcg(&arr[u])) != kNoTerm;
+}
+
 __device__ __forceinline__ NodeRec ld_rec(const NodeRec* p) {
   const int4 q = __ldcg(reinterpret_cast<const int4*>(p));
   NodeRec r;
@@ -277,8 +293,9 @@ full_sssp_kernel(ogr_graph g, ogr_state st, ogr_full::Job job, FWs w) {
   }
   const int32_t N = g.num_nodes;
   const int64_t E = g.num_edges;
-  const int32_t src = a.src, dst = a.dst;
-  if (src == dst) {
+  const bool multi = job.multi != 0;
+  const int32_t src = multi ? -1 : a.src, dst = multi ? -1 : a.dst;
+  if (!multi && src == dst) {
     if (leader) {
       ctl->res[0] = OGR_NO_PATH;
       ctl->res[1] = 0;
@@ -307,6 +324,7 @@ full_sssp_kernel(ogr_graph g, ogr_state st, ogr_full::Job job, FWs w) {
   int32_t gbase = __ldcg(&ctl->gbase);
   const int max_phase_natural = 2 * N + 4;
   const int max_phase = w.max_phases > 0 ? min(w.max_phases, max_phase_natural) : max_phase_natural;
+  bool cleared = false;
   if (gbase < 1 || gbase > 0x7fffffff - (max_phase_natural + 8)) {
     for (int64_t r = gtid; r < N; r += gthreads) {
       w.dirty[r] = 0;
@@ -316,7 +334,11 @@ full_sssp_kernel(ogr_graph g, ogr_state st, ogr_full::Job job, FWs w) {
       }
     }
     gbase = 1;
+    cleared = true;
   }
+  bool alive = true;
+  // the seeds' records are written below by one thread: the clearing must be over
+  if (multi && cleared) alive = grid_barrier(ctl, bar_target, sm, clk, &clk.init, w.bar_spin);
   const float* rc = st.rcost;
   if (rc == nullptr) {
     const int32_t* __restrict__ rev = g.rev;
@@ -325,7 +347,7 @@ full_sssp_kernel(ogr_graph g, ogr_state st, ogr_full::Job job, FWs w) {
     for (int64_t e = gtid; e < E; e += gthreads) out[e] = fcost[rev[e]];
     rc = w.rcost;
   }
-  if (leader) {
+  if (leader && !multi) {
     rec[src].reach = gbase;
     rec[src].sp = 0;
     w.fr[0][0] = make_int4(src, indptr[src], indptr[src + 1], __float_as_int(0.0f));
@@ -334,9 +356,44 @@ full_sssp_kernel(ogr_graph g, ogr_state st, ogr_full::Job job, FWs w) {
       ctl->tbits[i] = i == 0 ? 0ull : ~0ull;   // T of phase 0 = L(src) = 0
     }
     ctl->nlog = 0;
+  } else if (leader) {
+    // Multi-source: mark the targets, then put every seed in the first
+    // frontier with its label seed cost + penalty (T of phase 0 = the least).
+    int bad = 0, nf0 = 0;
+    unsigned long long t0 = ~0ull;
+    for (int i = 0; i < job.n_targets && !bad; ++i) {
+      const int32_t t = job.targets[i];
+      const double tc = job.target_cost[i];
+      if (t < 0 || t >= N || tc != tc) { bad = 1; break; }
+      unsigned long long* p = reinterpret_cast<unsigned long long*>(&w.mtgt[t]);
+      if (*p != kNoTerm) { bad = 1; break; }   // repeated target
+      *p = (unsigned long long)__double_as_longlong(tc);
+    }
+    for (int i = 0; i < job.n_seeds && !bad; ++i) {
+      const int32_t s0 = job.seeds[i];
+      const double sc = job.seed_cost[i];
+      if (s0 < 0 || s0 >= N || !(sc >= 0.0)) { bad = 1; break; }
+      unsigned long long* p = reinterpret_cast<unsigned long long*>(&w.mseed[s0]);
+      if (*p != kNoTerm) { bad = 1; break; }   // repeated seed
+      *p = (unsigned long long)__double_as_longlong(sc);
+      const float pen = ogr_node_penalty(st, a, s0);
+      rec[s0].reach = gbase;
+      rec[s0].sp = 0;
+      w.fr[0][nf0++] = make_int4(s0, indptr[s0], indptr[s0 + 1], __float_as_int(pen));
+      const unsigned long long lb = ogr_dbits(sc + (double)pen);
+      t0 = lb < t0 ? lb : t0;
+    }
+    for (int i = 0; i < 3; ++i) {
+      ctl->nfront[i] = (i == 0 && !bad) ? nf0 : 0;
+      ctl->tbits[i] = i == 0 ? t0 : ~0ull;
+      ctl->mk[i] = ~0ull;
+    }
+    ctl->nlog = 0;
+    ctl->merr = bad;
   }
-  bool alive = grid_barrier(ctl, bar_target, sm, clk, &clk.init, w.bar_spin);
+  if (alive) alive = grid_barrier(ctl, bar_target, sm, clk, &clk.init, w.bar_spin);
   int status = OGR_OK;
+  if (multi && __ldcg(&ctl->merr)) status = OGR_ERR_ARG;
   bool found = false;
   // With statistics requested the search goes on after dst is settled until
   // every node with a label <= L(dst) is settled (T > L(dst)): the IN bound
@@ -345,14 +402,14 @@ full_sssp_kernel(ogr_graph g, ogr_state st, ogr_full::Job job, FWs w) {
   bool dst_done = false;
   double ld = 0.0;
   int phase = 0;
-  while (alive) {
+  while (alive && status == OGR_OK) {
     const int b = phase % 3, bn = (phase + 1) % 3, bz = (phase + 2) % 3;
     const int32_t gp = gbase + 1 + phase;
     // the frontier length, T and (until it settles) dst's record, issued as
     // one batch of loads after the barrier
     const int nf = __ldcg(&ctl->nfront[b]);
     const unsigned long long tb = __ldcg(&ctl->tbits[b]);
-    if (!dst_done && phase > 0) {
+    if (!multi && !dst_done && phase > 0) {
       const NodeRec rd = ld_rec(&rec[dst]);
       if (rd.sp > gbase) {
         dst_done = true;
@@ -365,8 +422,8 @@ full_sssp_kernel(ogr_graph g, ogr_state st, ogr_full::Job job, FWs w) {
       }
     }
     if (nf == 0) {
-      if (dst_done)
-        found = true;
+      if (dst_done || multi)
+        found = true;            // multi-source: the target is chosen below
       else
         status = OGR_NO_PATH;
       break;
@@ -394,7 +451,8 @@ full_sssp_kernel(ogr_graph g, ogr_state st, ogr_full::Job job, FWs w) {
       // function of the in-neighbours settled before the phase.  A settle in
       // phase q writes dirty = q + 1 (values only grow; a settle of this very
       // phase may already show as gp + 1, which only adds a harmless pull).
-      const bool pull = !w.reuse || is_src || __ldcg(&w.dirty[v]) >= gp;
+      // (seeds are never marked dirty: a multi-source search always pulls)
+      const bool pull = multi || !w.reuse || is_src || __ldcg(&w.dirty[v]) >= gp;
       const bool one_pass = pull && f1 - f0 <= kSub;
       // pull: the lexicographic minimum of the candidates of the in-neighbours
       // settled before this phase; cin from the others.  One-pass rows keep
@@ -417,10 +475,13 @@ full_sssp_kernel(ogr_graph g, ogr_state st, ogr_full::Job job, FWs w) {
           i0 = indptr[u];
           i1 = indptr[u + 1];
         }
+        // multi-source: a target never relaxes anything, settled or not
+        const bool u_term = multi && is_term(w.mtgt, u);
         if (!(ru.sp > gbase && ru.sp < gp)) {
-          cin = fminf(cin, c);
+          if (!u_term) cin = fminf(cin, c);
           continue;
         }
+        if (u_term) continue;
         const float a32 = __double2float_rn((ru.lab + (double)c) + pd);
         if (!(a32 < kInf)) continue;
         if (ogr_key_lt(a32, ru.lab, u, ba, bl, bu)) { ba = a32; bl = ru.lab; bu = u; bc = c; }
@@ -439,6 +500,20 @@ full_sssp_kernel(ogr_graph g, ogr_state st, ogr_full::Job job, FWs w) {
       if (pull) {
         lv = is_src ? 0.0 : (bl + (double)bc) + pd;
         m32 = is_src ? 0.0f : ba;   // == float32(lv): the same expression
+        if (multi) {
+          // a seed's own candidate comes before every relaxation: it loses
+          // only to a strictly smaller float32 value
+          const double sc = __ldcg(&w.mseed[v]);
+          if ((unsigned long long)__double_as_longlong(sc) != kNoTerm) {
+            const double sl = sc + pd;
+            const float s32 = __double2float_rn(sl);
+            if (!(ba < s32)) {
+              lv = sl;
+              m32 = s32;
+              bu = -1;
+            }
+          }
+        }
       } else {
         lv = __ldcg(&rec[v].lab);
         m32 = __double2float_rn(lv);
@@ -465,6 +540,7 @@ full_sssp_kernel(ogr_graph g, ogr_state st, ogr_full::Job job, FWs w) {
         w.par[v] = is_src ? -1 : bu;
       }
       stage_push_tile(tile, sm, 1, sl == 0, v, w.log, &ctl->nlog);
+      if (multi && is_term(w.mtgt, v)) continue;   // a settled target is never expanded
       // mark the unreached out-neighbours and offer the candidate labels
       unsigned long long tl = ~0ull;
       for (int32_t fb = f0; fb < f1; fb += kSub) {   // same trip count on every lane (ballots inside)
@@ -511,14 +587,63 @@ full_sssp_kernel(ogr_graph g, ogr_state st, ogr_full::Job job, FWs w) {
   }
   if (!alive) status = OGR_ERR_TIMEOUT;
   const int nlog = __ldcg(&ctl->nlog);
+  // Multi-source: the settled target with the least (label + target cost,
+  // label, id) -- the first strict improvement in the heap's pop order.
+  int32_t tgt = dst;
+  if (multi && found) {
+    const double dinf = __longlong_as_double(0x7ff0000000000000ll);
+    unsigned long long k1 = ~0ull, k2 = ~0ull;
+    for (int pass = 0; pass < 3 && alive; ++pass) {
+      unsigned long long k = ~0ull;
+      for (int64_t i = gtid; i < nlog; i += gthreads) {
+        const int32_t r = __ldcg(&w.log[i]);
+        const double tc = __ldcg(&w.mtgt[r]);
+        if ((unsigned long long)__double_as_longlong(tc) == kNoTerm) continue;
+        const double lr = __ldcg(&rec[r].lab);
+        const double tot = lr + tc;
+        if (!(tot < dinf)) continue;
+        const unsigned long long kt = ogr_order_bits(tot), kl = ogr_order_bits(lr);
+        const unsigned long long x = pass == 0 ? kt : pass == 1 ? (kt == k1 ? kl : ~0ull)
+                                                               : (kt == k1 && kl == k2 ? (unsigned long long)r : ~0ull);
+        k = x < k ? x : k;
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long ok = __shfl_xor_sync(0xffffffffu, k, o);
+        k = ok < k ? ok : k;
+      }
+      if (lane == 0 && k != ~0ull) atomicMin(&ctl->mk[pass], k);
+      alive = grid_barrier(ctl, bar_target, sm, clk, &clk.e, w.bar_spin);
+      if (pass == 0) k1 = __ldcg(&ctl->mk[0]);
+      if (pass == 1) k2 = __ldcg(&ctl->mk[1]);
+      if (k1 == ~0ull) break;   // uniform: no target reached
+    }
+    if (!alive) {
+      status = OGR_ERR_TIMEOUT;
+      found = false;
+    } else if (k1 == ~0ull) {
+      status = OGR_NO_PATH;
+      found = false;
+    } else {
+      tgt = (int32_t)__ldcg(&ctl->mk[2]);
+    }
+  }
   // statistics: the rows of every node the sequential search pops before dst
   // (all of them are in the settled log)
-  if (found && want_stats) {
+  // A search that cannot reach dst pops every node it reaches (all of them in
+  // the log once the frontier is empty) and scans each one's row.
+  const bool exhausted = !multi && alive && status == OGR_NO_PATH;
+  if ((found || exhausted) && want_stats) {
     unsigned long long arcs = 0, pops = 0;
     for (int64_t i = gtid; i < nlog; i += gthreads) {
       const int32_t r = __ldcg(&w.log[i]);
+      if (multi) {   // the heap runs empty: every settled node popped, the non-targets expanded
+        ++pops;
+        if (!is_term(w.mtgt, r)) arcs += (unsigned long long)(indptr[r + 1] - indptr[r]);
+        continue;
+      }
       const double lr = __ldcg(&rec[r].lab);
-      if (lr < ld || (lr == ld && r < dst)) {
+      if (exhausted || lr < ld || (lr == ld && r < dst)) {
         arcs += (unsigned long long)(indptr[r + 1] - indptr[r]);
         ++pops;
       }
@@ -533,7 +658,7 @@ full_sssp_kernel(ogr_graph g, ogr_state st, ogr_full::Job job, FWs w) {
       atomicAdd(&job.stats[1], pops);
     }
     if (leader) {
-      atomicAdd(&job.stats[1], 1ull);
+      if (found && !multi) atomicAdd(&job.stats[1], 1ull);   // dst's own pop
       atomicAdd(&job.stats[2], (unsigned long long)N);
       atomicAdd(&job.stats[3], (unsigned long long)(phase + 1));
     }
@@ -541,6 +666,19 @@ full_sssp_kernel(ogr_graph g, ogr_state st, ogr_full::Job job, FWs w) {
   if (tid == 0) atomicMax(&g_full_prof[4], clk.e);
   examined = __reduce_add_sync(0xffffffffu, (unsigned)examined);
   if (lane == 0 && examined) atomicAdd(&g_full_prof[5], examined);
+  if (multi) {
+    // every CTA is past its reads of the marks: restore them for the next search
+    grid_barrier(ctl, bar_target, sm, clk, &clk.e, w.bar_spin);
+    const unsigned long long none = kNoTerm;
+    for (int64_t i = gtid; i < job.n_seeds; i += gthreads) {
+      const int32_t x = job.seeds[i];
+      if (x >= 0 && x < N) w.mseed[x] = __longlong_as_double((long long)none);
+    }
+    for (int64_t i = gtid; i < job.n_targets; i += gthreads) {
+      const int32_t x = job.targets[i];
+      if (x >= 0 && x < N) w.mtgt[x] = __longlong_as_double((long long)none);
+    }
+  }
   if (blockIdx.x != 0) return;
   // backtrace dst -> src in one walk (reversed into path_out), then CTA 0
   // turns it around
@@ -548,7 +686,7 @@ full_sssp_kernel(ogr_graph g, ogr_state st, ogr_full::Job job, FWs w) {
     int len = 0;
     if (found) {
       const int limit = min(path_cap, N);
-      int32_t c = dst;
+      int32_t c = tgt;
       while (c != -1 && len < limit) {
         path_out[len++] = c;
         c = __ldcg(&w.par[c]);
@@ -580,6 +718,11 @@ full_sssp_kernel(ogr_graph g, ogr_state st, ogr_full::Job job, FWs w) {
   atomicAdd(&g_full_prof[3], clk.init);
   atomicAdd(&g_full_prof[6], clk.wait);
   atomicAdd(&g_full_prof[7], t_end - clk.mark);
+}
+
+__global__ void fill_u64_kernel(unsigned long long* p, int64_t n, unsigned long long v) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    p[i] = v;
 }
 
 constexpr int kMaxDevices = 64;
@@ -631,7 +774,7 @@ int launch(const ogr_graph& g, const ogr_state& st, const Job& job, void* ws, cu
   w.max_phases = g_dbg_phases;
   ogr_full::Job jv = job;
   jv.gated = 0;
-  if (ogr_tile::enabled()) {
+  if (ogr_tile::enabled() && !job.multi) {
     const int trc = ogr_tile::launch(g, st, job, w.tile, w.ctl->res, &w.ctl->tile_gate, s);
     if (trc == OGR_OK)
       jv.gated = 1;              // the phase engine runs only if the net was handed over
@@ -701,8 +844,15 @@ extern "C" int ogr_full_workspace_init(void* ws, size_t bytes, int32_t num_nodes
   fws_layout(num_nodes, num_edges, (char*)ws, &w);
   // phase base 0: the first search clears the settle stamps; tile stamp 0:
   // the first tile search clears its node words
-  OGR_CUDA_TRY(cudaMemsetAsync(w.ctl, 0, sizeof(FCtl), ogr_stream(stream)));
-  OGR_CUDA_TRY(cudaMemsetAsync(w.tile, 0, ogr_tile::ctl_bytes(), ogr_stream(stream)));
+  cudaStream_t s = ogr_stream(stream);
+  OGR_CUDA_TRY(cudaMemsetAsync(w.ctl, 0, sizeof(FCtl), s));
+  OGR_CUDA_TRY(cudaMemsetAsync(w.tile, 0, ogr_tile::ctl_bytes(), s));
+  // no node is a multi-source seed or target until a search marks it
+  const int blocks = (int)std::min<int64_t>((num_nodes + 255) / 256, 152 * 8);
+  fill_u64_kernel<<<blocks, 256, 0, s>>>(reinterpret_cast<unsigned long long*>(w.mseed), num_nodes, kNoTerm);
+  OGR_LAUNCH_CHECK();
+  fill_u64_kernel<<<blocks, 256, 0, s>>>(reinterpret_cast<unsigned long long*>(w.mtgt), num_nodes, kNoTerm);
+  OGR_LAUNCH_CHECK();
   return OGR_OK;
 }
 
@@ -728,6 +878,41 @@ extern "C" int ogr_find_path_full(const ogr_graph* g, const ogr_state* st, const
   job.path_cap = path_cap;
   job.from_pass = 0;
   job.stats = reinterpret_cast<unsigned long long*>(stats);
+  cudaStream_t s = ogr_stream(stream);
+  const int rc = ogr_full::launch(*g, *st, job, ws, s);
+  if (rc != OGR_OK) return rc;
+  int32_t res[4];
+  OGR_CUDA_TRY(cudaMemcpyAsync(res, ogr_full::result_words(ws, g->num_nodes, g->num_edges), sizeof(res),
+                               cudaMemcpyDeviceToHost, s));
+  OGR_CUDA_TRY(cudaStreamSynchronize(s));
+  *path_len_out = res[0] == OGR_OK ? res[1] : 0;
+  return res[0];
+}
+
+extern "C" int ogr_find_path_full_multi(const ogr_graph* g, const ogr_state* st, const ogr_net_args* net,
+                                        const int32_t* seeds, const double* seed_cost, int32_t n_seeds,
+                                        const int32_t* targets, const double* target_cost, int32_t n_targets,
+                                        void* ws, size_t bytes, int32_t* path_out, int32_t path_cap,
+                                        int32_t* path_len_out, int64_t* stats, void* stream) {
+  if (!g || !st || !net || !ws || !path_out || !path_len_out || path_cap < 2) return OGR_ERR_ARG;
+  if (n_seeds < 0 || n_targets < 0 || (n_seeds > 0 && (!seeds || !seed_cost)) ||
+      (n_targets > 0 && (!targets || !target_cost)))
+    return OGR_ERR_ARG;
+  if (bytes < ogr_full::workspace_bytes(g->num_nodes, g->num_edges)) return OGR_ERR_CAPACITY;
+  *path_len_out = 0;
+  if (n_seeds == 0 || n_targets == 0) return OGR_NO_PATH;
+  ogr_full::Job job{};
+  job.a = *net;
+  job.path_out = path_out;
+  job.path_cap = path_cap;
+  job.stats = reinterpret_cast<unsigned long long*>(stats);
+  job.multi = 1;
+  job.seeds = seeds;
+  job.seed_cost = seed_cost;
+  job.n_seeds = n_seeds;
+  job.targets = targets;
+  job.target_cost = target_cost;
+  job.n_targets = n_targets;
   cudaStream_t s = ogr_stream(stream);
   const int rc = ogr_full::launch(*g, *st, job, ws, s);
   if (rc != OGR_OK) return rc;

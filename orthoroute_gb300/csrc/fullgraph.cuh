@@ -19,6 +19,17 @@ struct Job {
   const int64_t* pass_result;
   unsigned long long* stats;
   int32_t gated;   // 1: run only when the tile engine handed the net over
+  // multi-source multi-sink search (multi = 1; src / dst unused): distinct
+  // seeds start with label seed_cost + penalty and no parent, distinct
+  // targets settle but never expand; the result is the target with the least
+  // (label + target cost, label, node id).  Device arrays.
+  int32_t multi;
+  const int32_t* seeds;
+  const double* seed_cost;
+  int32_t n_seeds;
+  const int32_t* targets;
+  const double* target_cost;
+  int32_t n_targets;
 };
 
 size_t workspace_bytes(int32_t num_nodes, int64_t num_edges);

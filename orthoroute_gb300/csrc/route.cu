@@ -554,6 +554,7 @@ __device__ void sssp_roi(Shared& sh, const ogr_graph& g, const ogr_state& st, co
   const bool local = sh.local != 0;
   clk.mark(2);
   int phase = 0;
+  bool exhausted = false;   // the frontier ran out before dst settled
   if (sh.status == OGR_OK) {
     if constexpr (kMulti) {
       // the first recompute pass takes every seed (ROI order) from its initial
@@ -705,6 +706,7 @@ __device__ void sssp_roi(Shared& sh, const ogr_graph& g, const ogr_state& st, co
       if (tid == 0) atomicAdd(&g_stage[13], (unsigned long long)nd);
       const int nf = sh.nfront;
       if (nf == 0) {
+        if (!kMulti && !dst_done) exhausted = true;
         if (tid == 0 && !kMulti) {
           if (dst_done)
             sh.found = 1;
@@ -827,6 +829,27 @@ __device__ void sssp_roi(Shared& sh, const ogr_graph& g, const ogr_state& st, co
         atomicAdd(&stats_acc[2], (unsigned long long)R);
         atomicAdd(&stats_acc[3], (unsigned long long)(phase + 1));
       }
+    }
+  }
+  // A search that cannot reach dst pops every node it reaches and scans each
+  // one's row, as the heap does before it runs empty.
+  if (!kMulti && exhausted && stats_acc != nullptr) {
+    unsigned arcs = 0, pops = 0;
+    for (int r = tid; r < R; r += kThreads) {
+      if (node[r].st != ST_DONE) continue;
+      const int32_t rg = full ? r : roi[r];
+      arcs += (unsigned)(indptr[rg + 1] - indptr[rg]);
+      ++pops;
+    }
+    arcs = __reduce_add_sync(0xffffffffu, arcs);
+    pops = __reduce_add_sync(0xffffffffu, pops);
+    if (lane == 0) {
+      atomicAdd(&stats_acc[0], (unsigned long long)arcs);
+      atomicAdd(&stats_acc[1], (unsigned long long)pops);
+    }
+    if (tid == 0) {
+      atomicAdd(&stats_acc[2], (unsigned long long)R);
+      atomicAdd(&stats_acc[3], (unsigned long long)(phase + 1));
     }
   }
   // Arcs the sequential search scans before popping dst: the rows of all
@@ -1088,11 +1111,12 @@ path_apply_kernel(ogr_graph g, ogr_state st, const int32_t* path, int32_t len, i
 // exact small integers (and XOR ids), so paths may be applied by different
 // CTAs in any order and the state equals the sequential one.  Path k is
 // nodes[off[k] .. off[k+1]); its arcs go to arcs[2 * (off[k] - k) ..]; with a
-// store given, the path is also written to slot store_slot[k].
+// store given, the path, its length and its arcs are also written to slot
+// store_slot[k] (the per-net overuse sums read the slot's arcs).
 __global__ void __launch_bounds__(kApplyThreads)
 paths_commit_kernel(ogr_graph g, ogr_state st, const int32_t* nodes, const int32_t* off, const int32_t* net_ids,
                     int32_t n_paths, int32_t* arcs, int32_t* store_path, int32_t* store_len,
-                    const int32_t* store_slot, int32_t slot_cap, int32_t* status) {
+                    int32_t* store_arcs, const int32_t* store_slot, int32_t slot_cap, int32_t* status) {
   __shared__ int32_t s_via[kMaxViaNodes];
   __shared__ int s_nv, s_bad;
   const int tid = threadIdx.x, nt = blockDim.x;
@@ -1102,6 +1126,8 @@ paths_commit_kernel(ogr_graph g, ogr_state st, const int32_t* nodes, const int32
     const int32_t* path = nodes + o;
     const int hops = len - 1;
     int32_t* a_out = arcs + 2 * (int64_t)(o - k);
+    int32_t* a_store = (store_arcs != nullptr && len <= slot_cap)
+                           ? store_arcs + (int64_t)store_slot[k] * 2 * slot_cap : nullptr;
     if (tid == 0) { s_nv = 0; s_bad = 0; }
     __syncthreads();
     for (int i = tid; i < hops; i += nt) {
@@ -1113,6 +1139,10 @@ paths_commit_kernel(ogr_graph g, ogr_state st, const int32_t* nodes, const int32
       const int32_t r = g.rev[f];
       a_out[i] = f;
       a_out[hops + (hops - 1 - i)] = r;
+      if (a_store) {
+        a_store[i] = f;
+        a_store[hops + (hops - 1 - i)] = r;
+      }
       atomicAdd(&st.present[f], 1.0f);
       atomicAdd(&st.present[r], 1.0f);
     }
@@ -1367,7 +1397,8 @@ __device__ int commit_from(const ogr_graph& g, const ogr_state& st, const ogr_ne
 template <int L>
 __global__ void __launch_bounds__(kThreads, 1)
 window_pass_kernel(ogr_graph g, ogr_state st, ogr_net_table t, ogr_pass_args pa, ogr_roi_batch rb, char* slot_base,
-                   size_t slot_bytes, int32_t rmax, int32_t* scratch, char* ctl_base, Ws w, int32_t look) {
+                   size_t slot_bytes, int32_t rmax, int32_t* scratch, char* ctl_base, Ws w, int32_t look,
+                   unsigned long long* discarded) {
   __shared__ Shared sh;
   __shared__ int32_t s_via[kMaxViaNodes];
   __shared__ int s_flags[2];
@@ -1525,6 +1556,11 @@ window_pass_kernel(ogr_graph g, ogr_state st, ogr_net_table t, ogr_pass_args pa,
       // stays pending, to be searched again when its turn comes.
       const bool defer = !ws.inorder[ff];
       for (int m = defer ? ff : ff + 1; m < W && rc == OGR_OK; ++m) {   // undo the later rip-ups
+        if (discarded != nullptr && tid == 0) {
+          atomicAdd(&discarded[0], 1ull);
+          atomicAdd(&discarded[1], ws.stats[4 * m + 0]);
+          atomicAdd(&discarded[2], ws.stats[4 * m + 1]);
+        }
         const int32_t n = pa.order[ws.k[m]];
         const int32_t ol = t.store_len[n];
         if (ol >= 2)
@@ -1829,17 +1865,18 @@ extern "C" int ogr_extract_roi(const ogr_graph* g, const ogr_net_args* net, void
 
 extern "C" int ogr_paths_commit(const ogr_graph* g, const ogr_state* st, const int32_t* nodes, const int32_t* offsets,
                                 const int32_t* net_ids, int32_t n_paths, int32_t* arcs_out, int32_t* store_path,
-                                int32_t* store_len, const int32_t* store_slot, int32_t slot_cap, int32_t* status_dev,
-                                void* stream) {
+                                int32_t* store_len, int32_t* store_arcs, const int32_t* store_slot, int32_t slot_cap,
+                                int32_t* status_dev, void* stream) {
   if (!g || !st || n_paths < 0 || !status_dev) return OGR_ERR_ARG;
   if (n_paths == 0) return OGR_OK;
-  if (!nodes || !offsets || !net_ids || !arcs_out || ((store_path || store_len) && (!store_slot || slot_cap < 2)))
+  if (!nodes || !offsets || !net_ids || !arcs_out ||
+      ((store_path || store_len || store_arcs) && (!store_slot || slot_cap < 2)))
     return OGR_ERR_ARG;
   cudaStream_t s = ogr_stream(stream);
   OGR_CUDA_TRY(cudaMemsetAsync(status_dev, 0, sizeof(int32_t), s));
   const int grid = n_paths < 152 * 8 ? n_paths : 152 * 8;
   paths_commit_kernel<<<grid, kApplyThreads, 0, s>>>(*g, *st, nodes, offsets, net_ids, n_paths, arcs_out, store_path,
-                                                      store_len, store_slot, slot_cap, status_dev);
+                                                      store_len, store_arcs, store_slot, slot_cap, status_dev);
   OGR_LAUNCH_CHECK();
   return OGR_OK;
 }
@@ -1940,7 +1977,9 @@ extern "C" int ogr_route_pass(const ogr_graph* g, const ogr_state* st, const ogr
     int32_t* scratch = win->scratch;
     char* ctl = (char*)win->ctl;
     Ws wv = w;
-    void* args[] = {&gv, &sv, &tv, &pv, &rbv, &slot_base, &slot_bytes, &rmax, &scratch, &ctl, &wv, &lookv};
+    unsigned long long* discarded = reinterpret_cast<unsigned long long*>(win->discarded);
+    void* args[] = {&gv, &sv, &tv, &pv, &rbv, &slot_base, &slot_bytes, &rmax, &scratch, &ctl, &wv, &lookv,
+                    &discarded};
     const void* wk = nullptr;
     OGR_WITH_LANES(L, wk = (const void*)window_pass_kernel<L>);
     OGR_CUDA_TRY(cudaLaunchCooperativeKernel(wk, dim3(grid), dim3(kThreads), args, 0,

@@ -885,12 +885,15 @@ tile_sssp_kernel(ogr_graph g, ogr_state st, ogr_full::Job job, TWs w, Geo G, lon
   }
   if (!alive) status = OGR_ERR_TIMEOUT;
   if (failed) status = OGR_ERR_ITER_CAP;
-  // statistics: the nodes the sequential heap pops before dst, and their rows
-  if (found && job.stats) {
+  // statistics: the nodes the sequential heap pops before dst, and their rows;
+  // a search that cannot reach dst pops every node it reaches (every finite
+  // label is final once no label below the infinity is left)
+  const bool exhausted = status == OGR_NO_PATH;
+  if ((found || exhausted) && job.stats) {
     unsigned long long arcs = 0, pops = 0;
     for (int64_t i = gtid; i < N; i += gthreads) {
       const long long li = word_ticks(ld_word(&w.word[i]), stamp);
-      if (li < ld || (li == ld && i < dst)) {
+      if (exhausted ? li < kInf : (li < ld || (li == ld && i < dst))) {
         arcs += (unsigned long long)(g.indptr[i + 1] - g.indptr[i]);
         ++pops;
       }
@@ -905,7 +908,7 @@ tile_sssp_kernel(ogr_graph g, ogr_state st, ogr_full::Job job, TWs w, Geo G, lon
       atomicAdd(&job.stats[1], pops);
     }
     if (leader) {
-      atomicAdd(&job.stats[1], 1ull);
+      if (found) atomicAdd(&job.stats[1], 1ull);   // dst's own pop
       atomicAdd(&job.stats[2], (unsigned long long)N);
       atomicAdd(&job.stats[3], (unsigned long long)rounds);
     }

@@ -128,6 +128,8 @@ class Ops:
                        "ogr_route_workspace_init")
         self.path_buf = torch.empty(max(graph.N, 2), dtype=torch.int32, device=graph.device)
         self.stats = torch.zeros(4, dtype=torch.int64, device=graph.device)
+        # {searches, arcs, pops} of window searches whose results were undone
+        self.discarded = torch.zeros(3, dtype=torch.int64, device=graph.device)
         self.status = torch.zeros(1, dtype=torch.int32, device=graph.device)
         self.tally_out = torch.zeros(5, dtype=torch.int64, device=graph.device)
         self.layer_units = torch.zeros(graph.lattice.nz, dtype=torch.int64, device=graph.device)
@@ -314,6 +316,42 @@ class Ops:
         plane = self.g.lattice.plane
         return path, path[0] // plane, path[-1] // plane
 
+    def find_path_full_multi(self, src_seeds, dst_targets, net: _lib.NetArgs):
+        """Whole-lattice multi-source multi-sink search (ogr_find_path_full_multi)
+        on the state's costs and node penalty: seeds and targets are
+        ``(global node, cost)`` pairs; a repeated target keeps its last cost
+        (the reference builds a dict).  Returns ``(path, entry_layer,
+        exit_layer)`` or None."""
+        dev = self.g.device
+        tg = dict((int(n), float(c)) for n, c in dst_targets)
+        seeds = [(int(n), float(c)) for n, c in src_seeds]
+        if len({n for n, _ in seeds}) != len(seeds):
+            raise ValueError("repeated seed node")
+        if not seeds or not tg:
+            return None
+        sd = torch.as_tensor(np.asarray([n for n, _ in seeds], dtype=np.int32)).to(dev)
+        sc = torch.as_tensor(np.asarray([c for _, c in seeds], dtype=np.float64)).to(dev)
+        td = torch.as_tensor(np.asarray(list(tg), dtype=np.int32)).to(dev)
+        tc = torch.as_tensor(np.asarray(list(tg.values()), dtype=np.float64)).to(dev)
+        ws = self.full_workspace()
+        g = self.g.cgraph()
+        st = self.s.cstate()
+        n = C.c_int32(0)
+        rc = self.lib.ogr_find_path_full_multi(C.byref(g), C.byref(st), C.byref(net), _p(sd), _p(sc), int(sd.numel()),
+                                               _p(td), _p(tc), int(td.numel()), _p(ws), self.full_ws_bytes,
+                                               _p(self.path_buf), int(self.path_buf.numel()), C.byref(n),
+                                               _p(self.stats), self._sp())
+        _lib.check(rc, "ogr_find_path_full_multi")
+        self.counters["launches"] += 1
+        self.counters["search_launches"] += 1
+        self.counters["h2d_bytes"] += 12 * (len(seeds) + len(tg))
+        self.counters["d2h_bytes"] += 16 + 4 * max(0, n.value)
+        if rc == _lib.OGR_NO_PATH or n.value < 2:
+            return None
+        path = self.path_buf[: n.value].cpu().tolist()
+        plane = self.g.lattice.plane
+        return path, path[0] // plane, path[-1] // plane
+
     def extract_roi(self, net: _lib.NetArgs, slot: int = 0) -> np.ndarray:
         g = self.g.cgraph()
         out = torch.empty(self.g.N, dtype=torch.int32, device=self.g.device)
@@ -346,7 +384,8 @@ class Ops:
         st = self.s.cstate()
         _lib.check(self.lib.ogr_paths_commit(C.byref(g), C.byref(st), _p(d_nodes), _p(d_off), _p(d_ids), n, _p(arcs),
                                              _p(store.path) if store is not None else None,
-                                             _p(store.length) if store is not None else None, _p(d_slots),
+                                             _p(store.length) if store is not None else None,
+                                             _p(store.arcs) if store is not None else None, _p(d_slots),
                                              store.slot_cap if store is not None else 0, _p(self.status),
                                              self._sp()), "ogr_paths_commit")
         a = arcs.cpu().numpy().astype(np.int64)
@@ -422,18 +461,26 @@ class PathStore:
         return _lib.RoiBatch(self.bfs_slots, self.slot_bytes, self.qcap, _p(self.bfs_ws), _p(self.roi_pool),
                              _p(self.roi_len), self.roi_cap, _p(self.next), _p(self.roi_box))
 
-    def window_args(self) -> Optional[_lib.WindowArgs]:
+    def window_args(self, discarded: Optional[torch.Tensor] = None) -> Optional[_lib.WindowArgs]:
+        """discarded: device int64[3] that accumulates {searches, arcs, pops}
+        of window searches whose results were undone (those nets are searched
+        again)."""
         if not self.window_slots:
             return None
         return _lib.WindowArgs(self.window_slots, self.win_slot_bytes, _p(self.win_ws), _p(self.win_scratch),
-                               _p(self.win_ctl))
+                               _p(self.win_ctl), _p(discarded))
 
-    def set_path(self, idx: int, path):
+    def set_path(self, idx: int, path, arcs=None):
+        """Slot idx holds `path` and its arcs (forward then reverse, as the
+        commit returned them); an empty or one-node path clears the slot."""
         n = len(path)
         if n > self.slot_cap:
             raise RuntimeError("path longer than the path-store slot")
-        if n:
+        if n >= 2:
+            if arcs is None or len(arcs) != 2 * (n - 1):
+                raise ValueError("a stored path needs its 2 * (len - 1) arcs")
             self.path[idx, :n] = torch.as_tensor(np.asarray(path, dtype=np.int32)).to(self.path.device)
+            self.arcs[idx, :len(arcs)] = torch.as_tensor(np.asarray(arcs, dtype=np.int32)).to(self.arcs.device)
         self.length[idx] = n if n >= 2 else 0
 
 
@@ -469,7 +516,7 @@ def route_pass(ops: "Ops", store: PathStore, table: dict, order: np.ndarray, *, 
     if order_full is not None and np.any(order_full):
         full_flags = np.ascontiguousarray(order_full, dtype=np.uint8)
         full_ws, full_bytes = _p(ops.full_workspace()), ops.full_ws_bytes
-    win = store.window_args() if (batch_roi and windows) else None
+    win = store.window_args(ops.discarded) if (batch_roi and windows) else None
     rc = ops.lib.ogr_route_pass(C.byref(g), C.byref(st), C.byref(t), C.byref(a),
                                 C.byref(rb) if rb is not None else None, _p(ops.ws[0]), ops.ws_bytes,
                                 full_flags.ctypes.data if full_flags is not None else None, full_ws, full_bytes,

@@ -586,6 +586,11 @@ class PathFinderRouter:
         self._ov_idx = torch.empty(cap, dtype=torch.int32, device=dev)
         self._ov_val = torch.empty(cap, dtype=torch.float32, device=dev)
         self._ov_cnt = torch.zeros(1, dtype=torch.int32, device=dev)
+        # device barrel scan (persistent mode): node marks with a stamp per call, output lists
+        self._d_barrel_mark = torch.zeros(self.N, dtype=torch.int32, device=dev)
+        self._barrel_stamp = 0
+        self._barrel_cap = 0
+        self._barrel_ids = None
         self._reset_policy_state()
 
     def initialize_state(self):
@@ -618,13 +623,21 @@ class PathFinderRouter:
 
     def profile_reset(self):
         self.ops.reset_counters()
+        self.ops.discarded.zero_()
         self.stats = {"searches": 0, "arcs": 0, "pops": 0, "search_s": 0.0}
 
     def profile_snapshot(self):
+        """Counters since profile_reset.  `searches` counts accepted searches
+        (the reference's); `discarded_searches` the window searches whose
+        results were undone because an earlier member of their window failed
+        (those nets were searched again, and that search is in `searches`)."""
         c = dict(self.ops.counters)
+        disc = self.ops.discarded.cpu().numpy()
         return {"launches": int(c["launches"]), "h2d_bytes": int(c["h2d_bytes"]), "d2h_bytes": int(c["d2h_bytes"]),
                 "search_launches": int(c["search_launches"]), "search_kernel_ms": float(c["search_ms"]),
-                "searches": self.stats["searches"], "arcs": self.stats["arcs"], "pops": self.stats["pops"]}
+                "searches": self.stats["searches"], "arcs": self.stats["arcs"], "pops": self.stats["pops"],
+                "search_wall_s": float(self.stats["search_s"]),
+                "discarded_searches": int(disc[0]), "discarded_arcs": int(disc[1]), "discarded_pops": int(disc[2])}
 
     def _reset_policy_state(self):
         self.stagnation_counter = 0
@@ -863,19 +876,37 @@ class PathFinderRouter:
         u = self.node_use[self.node_use > 1]
         return int(u.sum(dtype=np.int64)) - u.size, int(u.size)
 
-    def _path_node_conflicts(self):
+    def _path_node_conflicts(self, shared_list=None):
         """Shared path nodes (``_detect_path_node_conflicts`` :10564-10606):
-        (pairs of nets sharing a node, the shared nodes, shared-node count per net)."""
+        (pairs of nets sharing a node, the shared nodes, shared-node count per net).
+        In persistent mode the (node, slot) entries of the stored paths on
+        shared nodes come from the device barrel scan (`shared_list`, or a
+        scan made here); the trivially routed one-node nets are added on the
+        host.  Otherwise the host flat view of all paths is filtered."""
         shared = self.node_use > 1
         if not shared.any():
             return set(), set(), {}
-        F = self._flat()
-        m = shared[F.nodes]
-        K = max(1, len(F.names))
-        key = _sorted_unique(F.nodes[m] * K + F.owner[m])
+        if getattr(self, "store", None) is not None:
+            if shared_list is None:
+                shared_list = self._barrel_scan()[4]
+            names = list(self._task_names)
+            single = [(n, p[0]) for n, p in self.net_paths.items() if p and len(p) == 1]
+            extra = [(len(names) + j, v) for j, (_, v) in enumerate(single) if shared[v]]
+            names += [n for n, _ in single]
+            nodes = shared_list[:, 0]
+            owner = shared_list[:, 1]
+            if extra:
+                nodes = np.concatenate([nodes, np.fromiter((v for _, v in extra), dtype=np.int64, count=len(extra))])
+                owner = np.concatenate([owner, np.fromiter((i for i, _ in extra), dtype=np.int64, count=len(extra))])
+        else:
+            F = self._flat()
+            m = shared[F.nodes]
+            names, nodes, owner = F.names, F.nodes[m], F.owner[m]
+        K = max(1, len(names))
+        key = _sorted_unique(nodes * K + owner)
         node, own = key // K, key % K
         cnt = np.bincount(own, minlength=K)
-        scores = {F.names[i]: int(cnt[i]) for i in np.flatnonzero(cnt).tolist()}
+        scores = {names[i]: int(cnt[i]) for i in np.flatnonzero(cnt).tolist()}
         pairs = set()
         if node.size:
             first = np.ones(node.size, dtype=bool)
@@ -897,56 +928,120 @@ class PathFinderRouter:
             shared_nodes = set()
         return pairs, shared_nodes, scores
 
+    def _barrel_scan(self):
+        """The device barrel scan of the stored paths (ogr_barrel_scan):
+        (conflicting hops, occ (node, net id)[], cnode (node, owner count,
+        owner xor)[], member (node, net id)[], shared (node, slot)[]) as
+        numpy arrays; the lists are grown and the scan repeated if a list
+        outgrew them."""
+        st, s = self.store, self.s
+        k = st.num_nets
+        dev = self.g.device
+        if self._barrel_ids is None or self._barrel_ids[0] != len(self.net_id_map):
+            ids = np.fromiter((self.net_id_map.get(n, -1) for n in self._task_names), dtype=np.int32, count=k)
+            self._barrel_ids = (len(self.net_id_map), torch.from_numpy(ids).to(dev))
+        ids = self._barrel_ids[1]
+        if self._barrel_cap == 0:
+            self._barrel_cap = 1 << 16
+        while True:
+            cap = self._barrel_cap
+            if getattr(self, "_d_barrel", None) is None or self._d_barrel[0] != cap:
+                self._d_barrel = (cap, torch.empty(2 * cap, dtype=torch.int32, device=dev),
+                                  torch.empty(3 * cap, dtype=torch.int32, device=dev),
+                                  torch.empty(2 * cap, dtype=torch.int32, device=dev),
+                                  torch.empty(2 * cap, dtype=torch.int32, device=dev),
+                                  torch.zeros(5, dtype=torch.int64, device=dev))
+            _, occ, cn, mem, sh, counts = self._d_barrel
+            self._barrel_stamp += 1
+            _lib.check(self.ops.lib.ogr_barrel_scan(
+                st.length.data_ptr(), st.path.data_ptr(), ids.data_ptr(), k, st.slot_cap, self.nx, self.ny,
+                s.owner_count.data_ptr(), s.owner_xor.data_ptr(), s.path_node_use.data_ptr(),
+                self._d_barrel_mark.data_ptr(), self._barrel_stamp, cap, occ.data_ptr(), cn.data_ptr(),
+                mem.data_ptr(), sh.data_ptr(), counts.data_ptr(), self.ops._sp()), "ogr_barrel_scan")
+            self.ops.counters["launches"] += 2
+            c = counts.cpu().numpy()
+            self.ops.counters["d2h_bytes"] += 40
+            need = int(c[1:].max())
+            if need <= cap:
+                break
+            self._barrel_cap = 1 << int(np.ceil(np.log2(need)))
+        n1, n2, n3, n4 = (int(x) for x in c[1:])
+        out = (occ[:2 * n1].view(n1, 2), cn[:3 * n2].view(n2, 3), mem[:2 * n3].view(n3, 2), sh[:2 * n4].view(n4, 2))
+        out = tuple(t.cpu().numpy().astype(np.int64) for t in out)
+        self.ops.counters["d2h_bytes"] += 4 * (2 * n1 + 3 * n2 + 2 * n3 + 2 * n4)
+        return (int(c[0]),) + out
+
     def _detect_barrels(self):
-        """Exact barrel conflicts + shared path nodes (``_detect_barrel_conflicts`` :10778-11111)."""
+        """Exact barrel conflicts + shared path nodes (``_detect_barrel_conflicts`` :10778-11111).
+
+        In persistent mode the per-hop work runs on the device over the path
+        store (ogr_barrel_scan) and only the conflicting endpoints, the conflict
+        nodes' barrel members and the shared path nodes come back; otherwise
+        it runs on the host over the flat view of the paths.  Both give
+        exact = the number of hops with a conflicting endpoint, the conflict
+        nodes (their history), and per (conflicting endpoint, other member of
+        its barrel) one score for both nets and one exact pair."""
         self.barrel_conflict_nets, self.barrel_owner_nets, self.barrel_victim_nets = set(), set(), set()
         self.physical_scores = defaultdict(int)
         self.exact_pairs = set()
-        F = self._flat()
+        device = getattr(self, "store", None) is not None
+        shared_list = None
         exact = 0
-        if F.names:
-            own = self._via_owner_of(F)
-            p = np.flatnonzero(F.same)          # hop (p, p+1) of one net
-            s, d = F.nodes[p], F.nodes[p + 1]
-            en = F.ids[F.owner[p]]
-            so, do = own[s], own[d]
-            sc = (so != -1) & (so != en)
-            dc = (do != -1) & (do != en)
-            cm = sc | dc
-            exact = int(cm.sum())
+        if device:
+            exact, occ, cn, mem, shared_list = self._barrel_scan()
             if exact:
-                names_by_id = list(self.net_id_map)
-                victims = _sorted_unique(en[cm])
-                cnodes = _sorted_unique(np.concatenate([s[sc], d[dc]]))
-                self._accumulate_history(cnodes)
-                vn, vid = F.via_members()
-                lo = np.searchsorted(vn, cnodes, "left")
-                hi = np.searchsorted(vn, cnodes, "right")
-                owners = _sorted_unique(vid[_expand_ranges(lo, hi)])
-                # every (conflicting endpoint, other member of its barrel) counts
-                # once for both nets and names one exact pair
-                qn = np.concatenate([s[sc], d[dc]])
-                qv = np.concatenate([en[sc], en[dc]])
-                lo = np.searchsorted(vn, qn, "left")
-                hi = np.searchsorted(vn, qn, "right")
-                j = _expand_ranges(lo, hi)
-                victim = np.repeat(qv, hi - lo)
-                other = vid[j]
-                keep = other != victim
-                victim, other = victim[keep], other[keep]
-                K = len(names_by_id)
-                cnt = np.bincount(victim, minlength=K) + np.bincount(other, minlength=K)
-                for i in np.flatnonzero(cnt).tolist():
-                    self.physical_scores[names_by_id[i]] += int(cnt[i])
-                for v in _sorted_unique(np.minimum(victim, other) * K + np.maximum(victim, other)).tolist():
-                    x, y = names_by_id[v // K], names_by_id[v % K]
-                    self.exact_pairs.add((x, y) if x <= y else (y, x))
-                vset = {names_by_id[i] for i in victims.tolist()}
-                oset = {names_by_id[i] for i in owners.tolist()}
-                self.barrel_victim_nets = vset
-                self.barrel_owner_nets = oset
-                self.barrel_conflict_nets = vset | oset
-        pairs, shared, pscores = self._path_node_conflicts()
+                qn, qv = occ[:, 0], occ[:, 1]
+                cnodes = _sorted_unique(cn[:, 0])
+                K = max(1, len(self.net_id_map))
+                one = cn[cn[:, 1] == 1]
+                key = _sorted_unique(np.concatenate([one[:, 0] * K + one[:, 2], mem[:, 0] * K + mem[:, 1]]))
+                vn, vid = key // K, key % K
+        else:
+            F = self._flat()
+            if F.names:
+                own = self._via_owner_of(F)
+                p = np.flatnonzero(F.same)          # hop (p, p+1) of one net
+                s, d = F.nodes[p], F.nodes[p + 1]
+                en = F.ids[F.owner[p]]
+                so, do = own[s], own[d]
+                sc = (so != -1) & (so != en)
+                dc = (do != -1) & (do != en)
+                cm = sc | dc
+                exact = int(cm.sum())
+                if exact:
+                    qn = np.concatenate([s[sc], d[dc]])
+                    qv = np.concatenate([en[sc], en[dc]])
+                    cnodes = _sorted_unique(qn)
+                    vn, vid = F.via_members()
+        if exact:
+            names_by_id = list(self.net_id_map)
+            victims = _sorted_unique(qv)
+            self._accumulate_history(cnodes)
+            lo = np.searchsorted(vn, cnodes, "left")
+            hi = np.searchsorted(vn, cnodes, "right")
+            owners = _sorted_unique(vid[_expand_ranges(lo, hi)])
+            # every (conflicting endpoint, other member of its barrel) counts
+            # once for both nets and names one exact pair
+            lo = np.searchsorted(vn, qn, "left")
+            hi = np.searchsorted(vn, qn, "right")
+            j = _expand_ranges(lo, hi)
+            victim = np.repeat(qv, hi - lo)
+            other = vid[j]
+            keep = other != victim
+            victim, other = victim[keep], other[keep]
+            K = len(names_by_id)
+            cnt = np.bincount(victim, minlength=K) + np.bincount(other, minlength=K)
+            for i in np.flatnonzero(cnt).tolist():
+                self.physical_scores[names_by_id[i]] += int(cnt[i])
+            for v in _sorted_unique(np.minimum(victim, other) * K + np.maximum(victim, other)).tolist():
+                x, y = names_by_id[v // K], names_by_id[v % K]
+                self.exact_pairs.add((x, y) if x <= y else (y, x))
+            vset = {names_by_id[i] for i in victims.tolist()}
+            oset = {names_by_id[i] for i in owners.tolist()}
+            self.barrel_victim_nets = vset
+            self.barrel_owner_nets = oset
+            self.barrel_conflict_nets = vset | oset
+        pairs, shared, pscores = self._path_node_conflicts(shared_list)
         self.path_node_pairs = set(pairs)
         self.path_node_scores = dict(pscores)
         if shared:
@@ -1048,7 +1143,7 @@ class PathFinderRouter:
         edges = self.ops.apply_path(path, self._net_id(name), sign, self._present_pres_fac, live=live)
         self._mark_nodes(name, path, sign)
         if self.store is not None:
-            self.store.set_path(self._task_index[name], path if sign > 0 else [])
+            self.store.set_path(self._task_index[name], path if sign > 0 else [], edges if sign > 0 else None)
         return edges
 
     def _order_nets(self, tasks):
@@ -1557,6 +1652,7 @@ class PathFinderRouter:
         self._tasks_all = tasks
         self._task_names = list(tasks)
         self._task_index = {n: i for i, n in enumerate(self._task_names)}
+        self._barrel_ids = None              # the store slots' net ids, rebuilt for this job
         if self.mode == "persistent":
             if self.store is None or self.store.num_nets != len(tasks):
                 self.store = PathStore(self.g, len(tasks),

@@ -310,6 +310,41 @@ def test_full_grid_search_unreachable_and_trivial():
     assert ops.find_path(ops.net_args(0, 3, 3, full_graph=True, penalty=False), engine="grid") is None
 
 
+def _walled_searches(g, s, ops, ref, engine, rng, n=3):
+    """Searches whose dst has every in-arc blocked: the heap pops every node
+    it reaches and scans each one's row before it runs empty, and the GPU's
+    counts must be those."""
+    N = g.N
+    base = _costs(3, g.E, rng)
+    for _ in range(n):
+        src, dst = (int(v) for v in rng.integers(0, ref.plane, size=2))
+        if src == dst:
+            continue
+        costs = base.copy()
+        costs[ref.indices == dst] = np.float32("inf")
+        s.total_cost.copy_(torch.from_numpy(costs))
+        ops.stats.zero_()
+        if engine == "roi":
+            r = roi_radius(src, dst, ref.nx, ref.plane)
+            roi, g2r = extract_roi_bfs(ref.indptr, ref.indices, N, src, dst, initial_radius=r)
+            got = ops.find_path(ops.net_args(0, src, dst, max_depth=min(r, 80), halo=2, penalty=False))
+        else:
+            roi = g2r = np.arange(N, dtype=np.int32)
+            got = ops.find_path(ops.net_args(0, src, dst, full_graph=True, penalty=False), engine=engine)
+        st = {}
+        want = find_path_roi_c(ref.indptr, ref.indices, src, dst, costs, roi, g2r, stats=st)
+        assert want is None and got is None, (src, dst)
+        arcs, pops = ops.stats.cpu().tolist()[:2]
+        assert st["settled"] > 100
+        assert (arcs, pops) == (st["scanned"], st["settled"]), (engine, src, dst)
+
+
+@pytest.mark.parametrize("engine", ["roi", "grid", "cta"])
+def test_failed_search_statistics_match_oracle(engine):
+    g, s, ops, ref = make(60, 40, 6)
+    _walled_searches(g, s, ops, ref, engine, np.random.default_rng(31))
+
+
 def test_find_path_replays_reference_net_trace():
     """Every recorded find_path_roi call of a real reference routing run."""
     meta = json.load(open(os.path.join(G, "golden.json")))["r0"]
@@ -530,8 +565,11 @@ def test_commit_paths_equals_one_by_one():
         assert a.tolist() == list(b)
     L = store.length.cpu().numpy()
     P = store.path.cpu().numpy()
-    for p, sl in zip(paths, slots):
+    A = store.arcs.cpu().numpy()
+    for p, sl, b in zip(paths, slots, one):
         assert L[sl] == len(p) and P[sl, :len(p)].tolist() == p
+        # the slot's arcs too: the per-net overuse sums of a restored state read them
+        assert A[sl, :2 * (len(p) - 1)].tolist() == list(b)
 
 
 @pytest.mark.parametrize("lanes,reuse", [(4, 0), (8, 0), (4, 1), (16, 1)])

@@ -114,3 +114,76 @@ def test_multisource_edge_cases():
     assert rc == _lib.OGR_ERR_ARG
     # the workspace stays usable after the error
     assert ops.find_path_multi([(a, 0.0)], [(a + 3, 0.0)], costs, roi)[0][-1] == a + 3
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_full_lattice_multisource_matches_oracle(seed):
+    """ogr_find_path_full_multi (the whole-lattice seeded search on all SMs)
+    against the oracle's find_path_multisource on the identity ROI: paths,
+    layers, nodes settled and arcs scanned, with the state's node penalty,
+    ties, blocked arcs and a seed that is also a target."""
+    from test_gpu_kernels import _costs, _penalty_state, make
+    dims = [(40, 30, 6), (64, 48, 8), (90, 60, 4)][seed % 3]
+    g, s, ops, ref = make(*dims)
+    rng = np.random.default_rng(300 + seed)
+    N = g.N
+    ident = np.arange(N, dtype=np.int32)
+    for case in range(4):
+        costs = _costs((seed + case) % 4, g.E, rng)
+        s.total_cost.copy_(torch.from_numpy(costs))
+        ns = _penalty_state(s, N, rng, 3) if case % 2 == 0 else None
+        pres_fac = float(rng.choice([1.0, 2.3]))
+        pen = ns.owner_penalty(ident, 3, pres_fac) if ns is not None else None
+        seeds, targets = _random_sets(rng, ident, int(rng.integers(1, 9)), int(rng.integers(1, 9)))
+        if case == 1:
+            targets.append((seeds[0][0], 0.9))
+        st = {}
+        want = find_path_multisource(ref.indptr, ref.indices, seeds, targets, costs, ident, ident, node_penalty=pen,
+                                     plane=ref.plane, stats=st)
+        ops.stats.zero_()
+        net = ops.net_args(3, 0, 1, full_graph=True, pres_fac=pres_fac, penalty=ns is not None)
+        got = ops.find_path_full_multi(seeds, targets, net)
+        assert got == (tuple(want) if want else None), (seed, case)
+        if want is not None:
+            arcs, pops = ops.stats.cpu().tolist()[:2]
+            assert (arcs, pops) == (st["scanned"], st["settled"]), (seed, case)
+    # the per-node seed / target marks are restored: a plain search right after is unaffected
+    from oracle.dijkstra import find_path_roi_c
+    costs = _costs(3, g.E, rng)
+    s.total_cost.copy_(torch.from_numpy(costs))
+    for _ in range(2):
+        a, b = (int(v) for v in rng.integers(0, ref.plane, size=2))
+        want = find_path_roi_c(ref.indptr, ref.indices, a, b, costs, ident, ident)
+        assert ops.find_path(ops.net_args(0, a, b, full_graph=True, penalty=False), engine="grid") == want
+
+
+def test_full_lattice_multisource_edge_cases():
+    from orthoroute_gb300 import _lib
+    from test_gpu_kernels import make
+    g, s, ops, ref = make(24, 20, 4)
+    s.total_cost.fill_(0.4)
+    net = ops.net_args(0, 0, 1, full_graph=True, penalty=False)
+    plane = ref.plane
+    a = plane + 1
+    # the cheapest target wins over a nearer dearer one, which is not expanded
+    res = ops.find_path_full_multi([(a, 0.0)], [(a + 1, 5.0), (a + 3, 0.0)], net)
+    assert res is not None and res[0][-1] == a + 3 and res[0][0] == a
+    # a target walled in by other targets is unreachable
+    assert ops.find_path_full_multi([(a, 0.0)], [(a, float("inf"))], net) is None
+    # argument errors at the C boundary: repeated target, negative seed cost
+    for seeds, targets in (([(a, 0.0)], [(a + 2, 0.0), (a + 2, 1.0)]), ([(a, -1.0)], [(a + 2, 0.0)])):
+        sd = torch.tensor([n for n, _ in seeds], dtype=torch.int32, device=g.device)
+        sc = torch.tensor([c for _, c in seeds], dtype=torch.float64, device=g.device)
+        td = torch.tensor([n for n, _ in targets], dtype=torch.int32, device=g.device)
+        tc = torch.tensor([c for _, c in targets], dtype=torch.float64, device=g.device)
+        n = C.c_int32(0)
+        ws = ops.full_workspace()
+        rc = ops.lib.ogr_find_path_full_multi(C.byref(g.cgraph()), C.byref(s.cstate()), C.byref(net),
+                                              sd.data_ptr(), sc.data_ptr(), 1, td.data_ptr(), tc.data_ptr(),
+                                              len(targets), ws.data_ptr(), ops.full_ws_bytes,
+                                              ops.path_buf.data_ptr(), int(ops.path_buf.numel()), C.byref(n), None,
+                                              None)
+        assert rc == _lib.OGR_ERR_ARG
+    # after the refused calls the marks are clean: the first case routes as before
+    res2 = ops.find_path_full_multi([(a, 0.0)], [(a + 1, 5.0), (a + 3, 0.0)], net)
+    assert res2 == res

@@ -132,3 +132,45 @@ def test_nets_overuse_matches_numpy(canonical):
             a = a[src[a] < dst[a]]
         assert sums[k].item() == over[a].sum()
         assert bool(hit[k].item()) == bool((over[a] > 0).any())
+
+
+@pytest.mark.parametrize("canonical", [0, 1])
+def test_per_net_overuse_after_restore_reads_restored_arcs(canonical):
+    """A best-state restore re-commits every path in one launch
+    (ogr_paths_commit).  The per-net overuse the stagnation rip-up ranks by
+    (ogr_nets_overuse over the path store's arcs) must then be that of the
+    restored paths, not of the paths the store held before."""
+    from orthoroute_gb300 import Lattice
+    from orthoroute_gb300.router import PathFinderConfig, PathFinderRouter
+    nx, ny, nz = 40, 30, 4
+    rng = np.random.default_rng(11)
+    reqs = []
+    while len(reqs) < 90:
+        x0, x1 = rng.integers(5, 35, size=2)
+        y0, y1 = rng.integers(5, 25, size=2)
+        if abs(int(x1) - int(x0)) + abs(int(y1) - int(y0)) >= 6:
+            reqs.append((f"N{len(reqs)}", int(y0) * nx + int(x0), int(y1) * nx + int(x1)))
+    R = PathFinderRouter(PathFinderConfig(max_iterations=1), mode="persistent", full_engine="grid")
+    R.initialize_lattice(Lattice(nx, ny, nz))
+    R.route_multiple_nets(reqs)
+    first = R._capture()
+    R.config = PathFinderConfig(max_iterations=4)
+    R.route_multiple_nets(reqs)
+    later = R._capture()
+    assert any(first.get(n) != later.get(n) for n in later), "the states must differ for the check to bite"
+    R._restore(first)
+    names, sums, hit = R._edge_over_device(canonical)
+    src = R.g.edge_src.cpu().numpy().astype(np.int64)
+    dst = R.g.indices.cpu().numpy().astype(np.int64)
+    arc_of = {(int(a), int(b)): e for e, (a, b) in enumerate(zip(src, dst))}
+    over = np.maximum(0.0, R.s.present.cpu().numpy() - R.s.capacity.cpu().numpy()).astype(np.float64)
+    assert over.sum() > 0
+    got = dict(zip(names, zip(sums.tolist(), hit.tolist())))
+    assert set(got) == {n for n, p in first.items() if p and len(p) >= 2}
+    for n, (s_, h_) in got.items():
+        p = first[n]
+        arcs = [arc_of[(u, v)] for u, v in zip(p[:-1], p[1:])] + [arc_of[(v, u)] for u, v in zip(p[:-1], p[1:])]
+        if canonical:
+            arcs = [e for e in arcs if src[e] < dst[e]]
+        assert s_ == float(over[arcs].sum()), n
+        assert bool(h_) == bool((over[arcs] > 0).any()), n

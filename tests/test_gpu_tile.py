@@ -10,7 +10,7 @@ pytestmark = pytest.mark.gpu
 
 from oracle.dijkstra import find_path_roi_c
 
-from test_gpu_kernels import _costs, _penalty_state, make
+from test_gpu_kernels import _costs, _penalty_state, _walled_searches, make
 
 
 def pstate(s, N, rng, net_id):
@@ -155,6 +155,13 @@ def test_tile_search_unreachable_and_trivial(tile_engine):
     s.total_cost.copy_(torch.from_numpy(costs))
     rng = np.random.default_rng(8)
     run_cases(ops, ref, costs, rng, 2)
+
+
+def test_tile_search_failed_search_statistics(tile_engine):
+    """A search that cannot reach dst counts every node it reaches, as the heap."""
+    g, s, ops, ref = make(60, 40, 6)
+    tile_engine(1.0)
+    _walled_searches(g, s, ops, ref, "grid", np.random.default_rng(32))
 
 
 def test_tile_search_many_in_a_row(tile_engine):
