@@ -267,7 +267,10 @@ def replica_value(ms: float, world: int) -> float:
 
 # --------------------------------------------------------------------- our arm
 def run_ours(args, cfg, rank, world):
+    import ctypes as C
+
     import torch
+    from orthoroute_gb300 import _lib
     from orthoroute_gb300.router import PathFinderConfig, PathFinderRouter
 
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
@@ -307,6 +310,8 @@ def run_ours(args, cfg, rank, world):
     sampler = ClockSampler()
     sampler.start()
     router.profile_reset()
+    full_prof = (C.c_int64 * 8)()
+    _lib.check(_lib.load().ogr_full_profile(full_prof, 1), "ogr_full_profile")   # reset the in-kernel counters
     start_ev = torch.cuda.Event(enable_timing=True)
     end_ev = torch.cuda.Event(enable_timing=True)
     start_ev.record()
@@ -320,6 +325,9 @@ def run_ours(args, cfg, rank, world):
     dev_ms = start_ev.elapsed_time(end_ev)
     clocks = sampler.stop()
     prof = router.profile_snapshot()
+    # whole-lattice searches: count, settle phases and in-kernel time (globaltimer, CTA 0)
+    _lib.check(_lib.load().ogr_full_profile(full_prof, 1), "ogr_full_profile")
+    full_n, full_phases, full_ns = int(full_prof[0]), int(full_prof[1]), int(full_prof[2])
     # end-to-end through the public API from host requests (fresh CSR build + state + read-back)
     e2e_t = []
     for _ in range(max(1, min(args.steps, 2))):
@@ -396,7 +404,12 @@ def run_ours(args, cfg, rank, world):
                        # negotiation policy, tallies, cost updates and their transfers
                        "routing_passes_s": round(prof["search_wall_s"] / max(1, args.steps), 3),
                        "host_policy_and_rest_s": round((ms / 1e3) - prof["search_wall_s"] / max(1, args.steps), 3),
-                       "job_s": round(ms / 1e3, 3)},
+                       "job_s": round(ms / 1e3, 3),
+                       # of the search kernels: the whole-lattice searches (in-kernel clock) and their phases
+                       "whole_lattice_searches_s": round(full_ns / 1e9 / max(1, args.steps), 3),
+                       "whole_lattice_searches": full_n // max(1, args.steps),
+                       "phases_per_whole_lattice_search": round(full_phases / max(1, full_n), 1),
+                       "us_per_phase": round(full_ns / 1e3 / max(1, full_phases), 3)},
         "searches_per_job": prof["searches"] // max(1, args.steps),
         # window searches whose results were undone (an earlier member of their window failed);
         # their nets were searched again and that search is the one counted above
@@ -516,8 +529,11 @@ class CpuSample:
             searches, iters = gpu_counts
             src = f"this GPU run of the bit-identical job: {searches} searches, {iters} iterations"
         else:
-            searches, iters = len(self.tasks) * self.cfg["iters"], self.cfg["iters"]
-            src = "no measured count: nets x iterations searches (an estimate)"
+            # no measured count: later iterations reroute an unmeasured subset of the nets, so
+            # only the first iteration's searches (every net once) are counted -- a lower bound
+            searches, iters = len(self.tasks), self.cfg["iters"]
+            src = ("no measured count: the first iteration's searches only (every net once), a lower bound "
+                   "of the job's searches")
         per = self.timed_search_s / max(1, self.timed_searches)
         v = per * searches + (self.policy_s or 0.0) * iters
         return v, (f"stratified sample of iteration 1: {self.timed_searches} searches ({per:.3f} s each) and one "

@@ -1532,14 +1532,25 @@ window_pass_kernel(ogr_graph g, ogr_state st, ogr_net_table t, ogr_pass_args pa,
     int ff = W;
     for (int m = 0; m < W; ++m)
       if (ws.st[m] != OGR_OK) { ff = m; break; }
-    if (ff == W) {
+    // With the pass's fallbacks used up (the count only grows, and only CTA 0
+    // writes it, before a barrier) a failed member takes no fallback: it stays
+    // unrouted with its old path ripped up, the state every member's search
+    // already saw, so every member's result is the sequential pass's and all
+    // of them are final -- in or out of order.
+    const bool no_fallback = (int)__ldcg(reinterpret_cast<const long long*>(&w.result[2])) >= pa.fallback_quota;
+    if (ff == W || no_fallback) {
       if (b < W) {
         const int32_t k = ws.k[b], n = pa.order[k];
-        const int rc = commit_from(g, st, t, pa, n, my_path, ws.len[b], s_via, s_flags);
         if (tid < 4) atomicAdd(&stats[tid], ws.stats[4 * b + tid]);
-        if (tid == 0) {
-          pa.net_status[k] = 0;
-          if (rc != OGR_OK) atomicExch(&c->error, rc);
+        if (ws.st[b] == OGR_OK) {
+          const int rc = commit_from(g, st, t, pa, n, my_path, ws.len[b], s_via, s_flags);
+          if (tid == 0) {
+            pa.net_status[k] = 0;
+            if (rc != OGR_OK) atomicExch(&c->error, rc);
+          }
+        } else if (tid == 0) {
+          t.store_len[n] = 0;
+          pa.net_status[k] = 1;
         }
       }
     } else if (b == 0) {

@@ -919,7 +919,6 @@ class PathFinderRouter:
                 ii, jj = np.triu_indices(k, 1)
                 pk.append((own[g[:, None] + ii] * K + own[g[:, None] + jj]).ravel())
             if pk:
-                names = F.names
                 for v in _sorted_unique(np.concatenate(pk)).tolist():
                     x, y = names[v // K], names[v % K]
                     pairs.add((x, y) if x <= y else (y, x))

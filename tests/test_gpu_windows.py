@@ -76,7 +76,9 @@ def test_windows_match_sequential_pass(seed, lanes, look):
         search_lanes(before)
         window_lookahead(look0)
     failed = 0
+    spent = False      # a pass whose fallbacks ran out while searches still failed
     for (s0, st0, l0, p0, a0), (s1, st1, l1, p1, a1) in zip(seq, win):
+        spent |= np.count_nonzero(s0 & 2) >= 5 and np.count_nonzero((s0 & 3) == 1) > 0
         np.testing.assert_array_equal(s0, s1)
         np.testing.assert_array_equal(st0, st1)
         np.testing.assert_array_equal(l0, l1)
@@ -88,3 +90,4 @@ def test_windows_match_sequential_pass(seed, lanes, look):
     for k in seq_state:
         np.testing.assert_array_equal(seq_state[k], win_state[k], err_msg=k)
     assert failed > 0, "the case should exercise failed searches and fallbacks"
+    assert spent, "the case should exhaust a pass's fallbacks (failed members then commit the window)"
