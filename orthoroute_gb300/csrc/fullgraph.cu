@@ -59,7 +59,6 @@ thread_local int g_dbg_phases = 0;
 struct FCtl {
   alignas(128) unsigned long long bar_count;   // monotone arrival counter
   alignas(128) int32_t bar_err;
-  uint32_t cmin_inv;                           // ~bits of the least arc cost (0: none yet)
   alignas(128) unsigned long long tbits[3];
   alignas(128) int32_t nfront[3];
   alignas(128) int32_t nlog;                   // settled-log length
@@ -348,20 +347,6 @@ full_sssp_kernel(ogr_graph g, ogr_state st, ogr_full::Job job, FWs w) {
     for (int64_t e = gtid; e < E; e += gthreads) out[e] = fcost[rev[e]];
     rc = w.rcost;
   }
-  {
-    // c_min, the least arc cost: a node nobody has reached yet can only be
-    // entered from a node settling at >= T over one more arc, so its label
-    // is at least fl(T + c_min).  Costs are >= 0; a -0.0 counts as 0.
-    unsigned mb = 0x7f800000u;
-#pragma unroll 4
-    for (int64_t e = gtid; e < E; e += gthreads) {
-      unsigned b = __float_as_uint(__ldcs(&fcost[e]));
-      b = (b & 0x80000000u) ? 0u : b;
-      mb = b < mb ? b : mb;
-    }
-    mb = __reduce_min_sync(0xffffffffu, mb);
-    if (lane == 0 && mb < 0x7f800000u) atomicMax(&ctl->cmin_inv, ~mb);
-  }
   if (leader && !multi) {
     rec[src].reach = gbase;
     rec[src].sp = 0;
@@ -414,8 +399,6 @@ full_sssp_kernel(ogr_graph g, ogr_state st, ogr_full::Job job, FWs w) {
   // every node with a label <= L(dst) is settled (T > L(dst)): the IN bound
   // can settle dst before cheaper nodes, which the heap pops earlier.
   const bool want_stats = job.stats != nullptr;
-  const unsigned cinv = __ldcg(&ctl->cmin_inv);
-  const double cmin = cinv == 0u ? 0.0 : (double)__uint_as_float(~cinv);
   bool dst_done = false;
   double ld = 0.0;
   int phase = 0;
@@ -446,7 +429,6 @@ full_sssp_kernel(ogr_graph g, ogr_state st, ogr_full::Job job, FWs w) {
       break;
     }
     const double T = __longlong_as_double((long long)tb);
-    const double tlo = T + cmin;   // lower bound of the label of any node not reached yet
     if (dst_done && T > ld) {
       found = true;
       break;
@@ -475,9 +457,7 @@ full_sssp_kernel(ogr_graph g, ogr_state st, ogr_full::Job job, FWs w) {
       // pull: the lexicographic minimum of the candidates of the in-neighbours
       // settled before this phase; cin from the others.  One-pass rows keep
       // each lane's neighbour data (stamps, penalty, CSR row) for the marking.
-      // cin: cheapest in-arc from a reached, unsettled node (label >= T); cun:
-      // from a node not reached yet (label >= tlo)
-      float ba = kInf, bc = kInf, cin = kInf, cun = kInf;
+      float ba = kInf, bc = kInf, cin = kInf;
       double bl = 0.0;
       int32_t bu = 0x7fffffff;
       int32_t u0 = -1, s0 = 0, r0 = 0, i0 = 0, i1 = 0;
@@ -498,12 +478,7 @@ full_sssp_kernel(ogr_graph g, ogr_state st, ogr_full::Job job, FWs w) {
         // multi-source: a target never relaxes anything, settled or not
         const bool u_term = multi && is_term(w.mtgt, u);
         if (!(ru.sp > gbase && ru.sp < gp)) {
-          if (!u_term) {
-            if (ru.reach == gbase)
-              cin = fminf(cin, c);
-            else
-              cun = fminf(cun, c);
-          }
+          if (!u_term) cin = fminf(cin, c);
           continue;
         }
         if (u_term) continue;
@@ -519,7 +494,6 @@ full_sssp_kernel(ogr_graph g, ogr_state st, ogr_full::Job job, FWs w) {
         const float oc = tile.shfl_xor(bc, o);
         if (ogr_key_lt(oa, ol, ou, ba, bl, bu)) { ba = oa; bl = ol; bu = ou; bc = oc; }
         cin = fminf(cin, tile.shfl_xor(cin, o));
-        cun = fminf(cun, tile.shfl_xor(cun, o));
       }
       double lv;
       float m32;
@@ -543,13 +517,10 @@ full_sssp_kernel(ogr_graph g, ogr_state st, ogr_full::Job job, FWs w) {
       } else {
         lv = __ldcg(&rec[v].lab);
         m32 = __double2float_rn(lv);
-        cin = __ldcg(&w.tcin[v]);   // both kinds, bounded by T (an in-neighbour may have been reached since)
+        cin = __ldcg(&w.tcin[v]);
         bu = __ldcg(&w.par[v]);
       }
-      // IN criterion: no unsettled in-neighbour can still offer a float32 key
-      // at or below m32
-      const float bnd = fminf(__double2float_rn((T + (double)cin) + pd), __double2float_rn((tlo + (double)cun) + pd));
-      const bool settle = (lv == T) || m32 < bnd;
+      const bool settle = (lv == T) || m32 < __double2float_rn((T + (double)cin) + pd);
       examined += (sl == 0);
       if (!settle) {
         stage_push_tile(tile, sm, 0, sl == 0, ent, frn, &ctl->nfront[bn]);
@@ -557,7 +528,7 @@ full_sssp_kernel(ogr_graph g, ogr_state st, ogr_full::Job job, FWs w) {
           atomicMin(&sm.tmin, ogr_dbits(lv));
           if (pull && w.reuse) {   // keep the pulled state; rec[v].lab is read by others only once settled
             rec[v].lab = lv;
-            w.tcin[v] = fminf(cin, cun);
+            w.tcin[v] = cin;
             w.par[v] = bu;
           }
         }
