@@ -463,6 +463,15 @@ __device__ void roi_build(Shared& sh, const ogr_graph& g, const ogr_net_args& a,
 //
 // kLanes lanes serve one node (its arcs, then a shuffle reduction), so a CTA
 // keeps 1024 / kLanes nodes in flight per round of a phase.
+// Arcs per lane that the local-adjacency stages of the ROI search load in one
+// batch: the first 12 arcs of a row (a lattice node has at most 10; at most 4
+// per lane, to stay in registers) are read at once, then the records they
+// name at once, so a row costs two dependent round trips instead of two per
+// kLanes arcs.  Slots past the degree lie in the row's 32-slot allocation and
+// are loaded but never used.
+constexpr int kBatchArcs = 12;
+static_assert(kBatchArcs <= kDMax, "a batch stays inside a local-adjacency row");
+
 template <bool kMulti = false, int kLanes = kSearchLanes>
 __device__ void sssp_roi(Shared& sh, const ogr_graph& g, const ogr_state& st, const ogr_net_args& a, const Ws& w,
                          const int32_t* roi, int32_t R, int32_t* path_out, int32_t path_cap,
@@ -588,9 +597,25 @@ __device__ void sssp_roi(Shared& sh, const ogr_graph& g, const ogr_state& st, co
       for (int i = grp; i < nb; i += kGroups) {
         const int32_t x = w.blist[i];
         if (local) {
+          constexpr int kB = (kBatchArcs + kSub - 1) / kSub < 4 ? (kBatchArcs + kSub - 1) / kSub : 4;
           const int dx = w.deg[x];
-          for (int k = sl; k < dx; k += kSub) {
-            const int32_t y = w.adj[(int64_t)x * kDMax + k];
+          const int32_t* arow = w.adj + (int64_t)x * kDMax;
+          int32_t yb[kB];
+#pragma unroll
+          for (int j = 0; j < kB; ++j) yb[j] = arow[sl + j * kSub];
+          int32_t sb[kB];
+#pragma unroll
+          for (int j = 0; j < kB; ++j) {
+            const bool ok = sl + j * kSub < dx && yb[j] >= 0;
+            sb[j] = ok ? node[yb[j]].st : ST_DONE;
+          }
+#pragma unroll
+          for (int j = 0; j < kB; ++j) {
+            if (sb[j] >= ST_DONE) continue;
+            if (atomicExch(&node[yb[j]].stamp, phase) != phase) w.dl[atomicAdd(&sh.ndirty, 1)] = yb[j];
+          }
+          for (int k = sl + kB * kSub; k < dx; k += kSub) {   // rows wider than a batch
+            const int32_t y = arow[k];
             if (y < 0 || node[y].st >= ST_DONE) continue;
             if (atomicExch(&node[y].stamp, phase) != phase) w.dl[atomicAdd(&sh.ndirty, 1)] = y;
           }
@@ -642,20 +667,42 @@ __device__ void sssp_roi(Shared& sh, const ogr_graph& g, const ogr_state& st, co
         }
         if (valid) {
           if (local) {
+            constexpr int kB = (kBatchArcs + kSub - 1) / kSub < 4 ? (kBatchArcs + kSub - 1) / kSub : 4;
             const int dy = w.deg[y];
-            for (int k = sl; k < dy; k += kSub) {
-              const int32_t u = w.adj[(int64_t)y * kDMax + k];
-              if (u < 0) continue;
-              const float c = w.acost[(int64_t)y * kDMax + k];
-              if (kMulti && node[u].st == ST_SINK) continue;   // targets relax nothing
-              if (node[u].st != ST_DONE) {
+            const int32_t* arow = w.adj + (int64_t)y * kDMax;
+            const float* crow = w.acost + (int64_t)y * kDMax;
+            int32_t ub[kB];
+            float cb[kB];
+#pragma unroll
+            for (int j = 0; j < kB; ++j) {
+              ub[j] = arow[sl + j * kSub];
+              cb[j] = crow[sl + j * kSub];
+            }
+            int32_t sb[kB];
+            double lb[kB];
+#pragma unroll
+            for (int j = 0; j < kB; ++j) {
+              const bool ok = sl + j * kSub < dy && ub[j] >= 0;
+              sb[j] = ok ? node[ub[j]].st : -1;
+              lb[j] = ok ? node[ub[j]].lab : 0.0;
+            }
+            auto relax = [&](int32_t u, float c, int32_t su, double lu) {
+              if (kMulti && su == ST_SINK) return;   // targets relax nothing
+              if (su != ST_DONE) {
                 cin = fminf(cin, c);
-                continue;
+                return;
               }
-              const double lu = node[u].lab;
               const float a32 = __double2float_rn((lu + (double)c) + pd);
-              if (!(a32 < kInf)) continue;
+              if (!(a32 < kInf)) return;
               if (ogr_key_lt(a32, lu, u, ba, bl, bu)) { ba = a32; bl = lu; bu = u; bc = c; }
+            };
+#pragma unroll
+            for (int j = 0; j < kB; ++j)
+              if (sb[j] >= 0) relax(ub[j], cb[j], sb[j], lb[j]);
+            for (int k = sl + kB * kSub; k < dy; k += kSub) {   // rows wider than a batch
+              const int32_t u = arow[k];
+              if (u < 0) continue;
+              relax(u, crow[k], node[u].st, node[u].lab);
             }
           } else {
             const int32_t yg = full ? y : roi[y];
