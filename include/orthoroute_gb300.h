@@ -449,7 +449,7 @@ int ogr_route_pass(const ogr_graph* g, const ogr_state* st, const ogr_net_table*
  * 8219-8262, into find_path_roi :2451-2548 with roi_nodes = all nodes).  Same
  * result, statistics and status codes as ogr_find_path with
  * net->full_graph = 1, computed by one cooperative launch on all SMs.  The
- * workspace (about 44 bytes per node + 4 per arc) is initialised once with
+ * workspace (about 108 bytes per node + 4 per arc) is initialised once with
  * ogr_full_workspace_init; a search rewrites the 8-byte key word of every
  * node and otherwise touches only the nodes it reaches.
  * OGR_ERR_TIMEOUT: a grid barrier gave up (not expected; the launch is
