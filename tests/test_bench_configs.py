@@ -48,3 +48,24 @@ def test_bga_backplane_workload():
     ys = np.array([_coords(b, nx)[1] for b in balls])
     assert abs(xs.mean() - nx / 2) < 2 and abs(ys.mean() - ny / 2) < 2  # centred 40x40 field
     assert xs.max() - xs.min() == pytest.approx(39 * 2.5, abs=1)
+
+
+def test_cpu_sample_scales_by_measured_counts_or_a_lower_bound():
+    """The CPU baseline's job time = time per sampled search x the job's
+    searches + policy time per iteration; the count is the oracle's own (the
+    committed trajectory), else this GPU run's, else only the first
+    iteration's searches (every net once), which can only understate it."""
+    cs = object.__new__(bench.CpuSample)
+    cs.small = False
+    cs.timed_search_s, cs.timed_searches, cs.policy_s = 10.0, 20, 2.0
+    cs.name, cs.cfg, cs.tasks = "c1", bench.CONFIGS["c1"], {f"N{i}": (0, 1) for i in range(2000)}
+    fx = bench.trajectory_fixture("c1")
+    assert fx is not None
+    v, desc = cs.estimate()
+    assert v == pytest.approx(0.5 * fx["searches"] + 2.0 * fx["result"]["iterations"])
+    assert "oracle's own run" in desc
+    cs.name, cs.cfg, cs.tasks = "c3", bench.CONFIGS["c3"], {f"N{i}": (0, 1) for i in range(4800)}
+    v, desc = cs.estimate(gpu_counts=(7000, 2))
+    assert v == pytest.approx(0.5 * 7000 + 2.0 * 2) and "GPU run" in desc
+    v, desc = cs.estimate()
+    assert v == pytest.approx(0.5 * 4800 + 2.0 * bench.CONFIGS["c3"]["iters"]) and "lower bound" in desc
