@@ -144,7 +144,7 @@ struct Sm {
   int32_t gid[kMaxNodes];                // global id of each tile node
   int32_t f0[kMaxNodes];                 // global CSR row start of each tile node
   uint32_t rmask[kMaxNodes / 8];         // 4 bits per node: ring sides (W, E, S, N) its arcs reach
-  uint32_t wl[2][kMaxNodes / 32];        // worklists
+  uint32_t wl[3][kMaxNodes / 32];        // activation bitmaps of three consecutive iterations
   uint32_t chg[kMaxNodes / 32];          // label or winner changed since the load
   uint32_t lchg[kMaxNodes / 32];         // label changed since the load
   int32_t scan[kT / 32 + 1];
@@ -477,6 +477,7 @@ __device__ bool process_tile(Sm& sm, const Geo& G, int t, const ogr_graph& g, co
   for (int k = tid; k < nwords; k += kT) {
     sm.wl[0][k] = 0u;
     sm.wl[1][k] = 0u;
+    sm.wl[2][k] = 0u;
     sm.chg[k] = 0u;
     sm.lchg[k] = 0u;
   }
@@ -489,13 +490,17 @@ __device__ bool process_tile(Sm& sm, const Geo& G, int t, const ogr_graph& g, co
     tm0 = t1;
   }
   // Iteration 0 evaluates every node; iteration k evaluates the nodes with
-  // an in-tile in-neighbour whose label changed in iteration k - 1 (the
-  // bitmap wl[prev], pulled, so no two threads write one word).  Node
-  // i = base + tid: a warp owns one 32-bit word of every bitmap and writes it
-  // from a ballot.  One barrier per iteration.
+  // an in-tile in-neighbour whose label changed in iteration k - 1.  A node
+  // whose label changes marks its in-tile neighbours in the next
+  // iteration's bitmap (lattice arcs come in pairs, so its in-neighbours are
+  // the nodes it feeds): a node's activity is one bit, not a walk over its
+  // in-neighbours.  Bitmaps rotate over three buffers: iteration k reads
+  // wl[k % 3], marks wl[(k + 1) % 3] and clears wl[(k + 2) % 3], whose last
+  // reader finished at the previous barrier.  Node i = base + tid: a warp
+  // owns one 32-bit word of chg / lchg and writes it from a ballot.  One
+  // barrier per iteration.
   const int lane = tid & 31, wid = tid >> 5;
   unsigned nev_all = 0;
-  int cur = 0;
   const int cap = 4 * nt + 64;
   int it = 0;
   for (;; ++it) {
@@ -503,7 +508,8 @@ __device__ bool process_tile(Sm& sm, const Geo& G, int t, const ogr_graph& g, co
       if (tid == 0) fail(w.ctl, kWhyLocalCap);
       return false;
     }
-    const int prev = cur ^ 1;
+    const int rd = it % 3, mk = (it + 1) % 3, clr = (it + 2) % 3;
+    for (int k = tid; k < nwords; k += kT) sm.wl[clr][k] = 0u;
     bool changed = false, bad = false;
     unsigned nev = 0;
     for (int base = 0; base < nt; base += kT) {
@@ -513,16 +519,7 @@ __device__ bool process_tile(Sm& sm, const Geo& G, int t, const ogr_graph& g, co
         const long long li = sm.lab[i];
         bool act = li >= wstart && i != sm.srcl;    // settled nodes and the source never change
         const int r0 = sm.rs[i], r1 = sm.rs[i + 1];
-        if (act && it > 0) {
-          act = false;
-          for (int k = r0; k < r1; ++k) {
-            const int s = sm.anb[k];
-            if (s < nt && ((sm.wl[prev][s >> 5] >> (s & 31)) & 1u)) {
-              act = true;
-              break;
-            }
-          }
-        }
+        if (act && it > 0) act = (sm.wl[rd][i >> 5] >> (i & 31)) & 1u;
         if (act) {
           ++nev;
           const long long pt = sm.pen[i];
@@ -588,6 +585,10 @@ __device__ bool process_tile(Sm& sm, const Geo& G, int t, const ogr_graph& g, co
             if (nl != li) {
               sm.lab[i] = nl;
               lch = true;
+              for (int k = r0; k < r1; ++k) {   // wake the in-tile nodes this one feeds
+                const int s2 = sm.anb[k];
+                if (s2 < nt) atomicOr(&sm.wl[mk][s2 >> 5], 1u << (s2 & 31));
+              }
             }
           }
         }
@@ -596,7 +597,6 @@ __device__ bool process_tile(Sm& sm, const Geo& G, int t, const ogr_graph& g, co
       const unsigned bc_ = __ballot_sync(0xffffffffu, ch);
       const int word = (base >> 5) + wid;
       if (lane == 0 && word < nwords) {
-        sm.wl[cur][word] = bl_;
         sm.chg[word] |= bc_;
         sm.lchg[word] |= bl_;
       }
@@ -611,7 +611,6 @@ __device__ bool process_tile(Sm& sm, const Geo& G, int t, const ogr_graph& g, co
       if (tid == 0) fail(w.ctl, kWhyArcCost);
       return false;
     }
-    cur = prev;
     if (!any) break;
   }
   nev_all = __reduce_add_sync(0xffffffffu, nev_all);
