@@ -794,8 +794,9 @@ tile_sssp_kernel(ogr_graph g, ogr_state st, ogr_full::Job job, TWs w, Geo G, lon
       break;
     }
     const long long B = (T > kInf - delta) ? kInf : T + delta;
-    // round 1: tiles with an unsettled label below B, and the tiles beside
-    // a side whose boundary holds a label that becomes a source now
+    // the window's first grid step: tiles with an unsettled label below B,
+    // and the tiles beside a side whose boundary holds a label that becomes
+    // a source now
     for (int k = tid; k < nab; k += kT) abits[k] = 0u;
     __syncthreads();
     for (int t = tid; t < G.ntiles; t += kT) {
@@ -819,7 +820,7 @@ tile_sssp_kernel(ogr_graph g, ogr_state st, ogr_full::Job job, TWs w, Geo G, lon
       else if (d < 5) w.side[wb][4 * (int64_t)t + d - 1] = __ldcg(&w.side[rb][4 * (int64_t)t + d - 1]);
     }
     __syncthreads();
-    int nlist = -1;   // -1: round 1 reads the bitmap
+    int nlist = -1;   // -1: the window's first grid step reads the bitmap
     int wrounds = 0;
     while (true) {
       if (++wrounds > max_rounds || rounds >= max_total) {
