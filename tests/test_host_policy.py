@@ -279,3 +279,89 @@ def test_parse_requests_like_the_reference():
     res = R.PathFinderRouter._no_routable_nets([("X", 2, 2), ("Y", 1.5, 3)])
     assert res["error_code"] == "NO-ROUTABLE-NETS" and res["excluded_net_ids"] == ["X", "Y"]
     assert res["total_nets"] == 2 and not res["success"]
+
+
+def _scan_lists(h, paths, task_names):
+    """What ogr_barrel_scan returns for these stored paths (its semantics in
+    numpy): conflicting hops; (endpoint, net id) per conflicting endpoint;
+    (node, owner count, owner xor) per distinct conflict node; (node, net id)
+    of the via hops spanning a conflict node owned by several nets; (node,
+    slot) per stored-path node used more than once."""
+    cnt = np.zeros(h.N, dtype=np.int64)
+    xr = np.zeros(h.N, dtype=np.int64)
+    spans = {}
+    for n in task_names:
+        p = paths[n]
+        if len(p) < 2:
+            continue
+        nid = h.net_id_map[n]
+        nodes = set()
+        for u, v in zip(p, p[1:]):
+            zu, ru = divmod(u, h.plane)
+            zv, rv = divmod(v, h.plane)
+            if ru == rv and zu != zv:
+                nodes.update(z * h.plane + ru for z in range(min(zu, zv), max(zu, zv) + 1))
+        spans[n] = nodes
+        for nd in nodes:
+            cnt[nd] += 1
+            xr[nd] ^= nid
+    owner = np.where(cnt == 0, -1, np.where(cnt == 1, xr, -2))
+    exact, occ, cnodes, seen = 0, [], [], set()
+    for n in task_names:
+        p = paths[n]
+        if len(p) < 2:
+            continue
+        en = h.net_id_map[n]
+        for u, v in zip(p, p[1:]):
+            sc = owner[u] != -1 and owner[u] != en
+            dc = owner[v] != -1 and owner[v] != en
+            exact += int(sc or dc)
+            for x, c in ((u, sc), (v, dc)):
+                if c:
+                    occ.append((x, en))
+                    if x not in seen:
+                        seen.add(x)
+                        cnodes.append((x, int(cnt[x]), int(xr[x])))
+    members = [(nd, h.net_id_map[n]) for n in task_names if len(paths[n]) >= 2
+               for nd in spans[n] if nd in seen and cnt[nd] >= 2]
+    shared = [(x, k) for k, n in enumerate(task_names) if len(paths[n]) >= 2
+              for x in paths[n] if h.node_use[x] > 1]
+    arr = lambda rows, w: np.asarray(rows, dtype=np.int64).reshape(-1, w)
+    return exact, arr(occ, 2), arr(cnodes, 3), arr(members, 2), arr(shared, 2)
+
+
+@pytest.mark.parametrize("seed", range(4))
+def test_barrel_lists_from_the_device_give_the_host_result(seed):
+    """_detect_barrels's persistent-mode branch (the device scan's lists, then
+    sorts on the host) against its flat-view branch and the oracle's loops."""
+    h, paths, esrc, edst, edges = _routed(seed)
+    task_names = [n for n, p in paths.items() if len(p) != 1]   # one-node nets are routed trivially
+    h._task_names = task_names
+    lists = _scan_lists(h, paths, task_names)
+    assert lists[0] > 0 and len(lists[3]) > 0 and len(lists[4]) > 0
+    results = []
+    for device in (False, True):
+        h._hist_mask.fill(False)
+        h._hist_iter = None
+        h.node_history.fill(0)
+        h.s.node_history.zero_()
+        h.store = object() if device else None
+        if device:
+            h._barrel_scan = lambda: lists
+        got = h._detect_barrels()
+        results.append((got, set(h.barrel_victim_nets), set(h.barrel_owner_nets), set(h.barrel_conflict_nets),
+                        set(h.exact_pairs), set(h.path_node_pairs), dict(h.path_node_scores),
+                        dict(h.physical_scores), h.node_history.copy()))
+    host, dev = results
+    for a, b in zip(host, dev):
+        if isinstance(a, np.ndarray):
+            np.testing.assert_array_equal(a, b)
+        else:
+            assert a == b
+    ns = NodeState(h.N, h.nx, h.plane)
+    ns.rebuild_owner([(h.net_id_map[n], p) for n, p in paths.items()])
+    for p in paths.values():
+        if len(p) >= 2:
+            ns.mark_use(p)
+    want, info = detect_barrel_conflicts(esrc, edst, ns, paths, edges, h.net_id_map, h.iteration)
+    assert dev[0] == want and dev[4] == info["exact_pairs"] and dev[3] == info["conflict_nets"]
