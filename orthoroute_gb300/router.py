@@ -729,6 +729,21 @@ class PathFinderRouter:
             self._flat_view = f
         return f
 
+    def _mark_many(self, arrays, sign):
+        """_mark_nodes of many paths at once: each path's distinct nodes count once."""
+        arrays = [a for a in arrays if a.size]
+        if not arrays:
+            return
+        P = len(arrays)
+        key = _sorted_unique(np.concatenate(arrays) * P +
+                             np.repeat(np.arange(P, dtype=np.int64), [a.size for a in arrays]))
+        cnt = np.bincount(key // P, minlength=self.N)
+        hit = np.flatnonzero(cnt)
+        if sign > 0:
+            self.node_use[hit] += cnt[hit].astype(self.node_use.dtype)
+        else:
+            self.node_use[hit] = np.maximum(self.node_use[hit].astype(np.int64) - cnt[hit], 0).astype(self.node_use.dtype)
+
     def _mark_nodes(self, name, path, sign, array=None):
         """path_node_use of one net's path (``_mark_path_node_use`` :4635);
         the via-barrel ownership is derived from the paths when read."""
@@ -1150,10 +1165,14 @@ class PathFinderRouter:
         names, sums, _ = self._edge_over(over_idx, over_val)
         cong_of = {n: float(sums[i]) / max(1, self.net_to_edges[n].size) for i, n in enumerate(names)}
         scores = []
+        d3 = self._dist3 if getattr(self, "_dist3", None) is not None else {}
+        self._dist3 = d3
         for name, (s, d) in tasks.items():
-            sx, sy, sz = self.idx_to_coord(s)
-            dx, dy, dz = self.idx_to_coord(d)
-            dist = abs(dx - sx) + abs(dy - sy) + abs(dz - sz)
+            dist = d3.get(name)
+            if dist is None:
+                sx, sy, sz = self.idx_to_coord(s)
+                dx, dy, dz = self.idx_to_coord(d)
+                dist = d3[name] = abs(dx - sx) + abs(dy - sy) + abs(dz - sz)
             cong = cong_of.get(name, 0.0)
             scores.append((dist * 3 * (cong + 1), name))
         owners, victims = self.barrel_owner_nets, self.barrel_victim_nets
@@ -1191,7 +1210,8 @@ class PathFinderRouter:
             self.ops.live_begin(self._present_pres_fac)
         if self.full_engine_request == "auto" and self.tuning is None:
             self._autotune(all_tasks)
-        # the engine knob is process-wide: every pass sets this router's choice
+        # the engine knob is per host thread, shared by the routers of a thread:
+        # every pass sets this router's choice
         from . import autotune
         autotune.full_tile(1 if self.full_tile_delta > 0 else 0, self.full_tile_delta)
         if self.mode == "persistent":
@@ -1221,30 +1241,41 @@ class PathFinderRouter:
         return routed, len(all_tasks) - routed
 
     def _net_table(self, bonus):
-        """Per-net search parameters of this pass (``extract_roi`` :2240-2255)."""
+        """Per-net search parameters of this pass (``extract_roi`` :2240-2255).
+        Endpoints, Manhattan lengths and the full-graph flag are fixed for a
+        job and uploaded once; ids once every net has one (they are assigned
+        in first-use order, as before: this pass's order, then task order);
+        ROI depth and halo whenever the stagnation bonus changes."""
         names = self._task_names
         n = len(names)
-        src = np.empty(n, dtype=np.int32)
-        dst = np.empty(n, dtype=np.int32)
-        nid = np.empty(n, dtype=np.int32)
-        full = np.empty(n, dtype=np.int32)
-        depth = np.empty(2 * n, dtype=np.int32)
-        halo = np.empty(2 * n, dtype=np.int32)
-        for i, name in enumerate(names):
-            s_, d_ = self._tasks_all[name]
-            src[i], dst[i] = s_, d_
-            nid[i] = self._net_id(name)
-            dist = self._manhattan(s_, d_)
-            full[i] = 1 if dist >= ROI_THRESHOLD_STEPS else 0
-            for j, b in enumerate((bonus, bonus * 2)):
-                radius = max(60, int(dist * 0.75 + b * 2.0))
-                depth[2 * i + j] = min(int(radius + b * 2.0), 80)
-                halo[2 * i + j] = min(16, 2 + int(max(0.0, b) / 0.6))
         dev = self.g.device
-        table = {k: torch.from_numpy(v).to(dev) for k, v in
-                 dict(src=src, dst=dst, id=nid, full=full, depth=depth, halo=halo).items()}
-        table["full_host"] = full.astype(np.uint8)
-        return table
+        c = self._table_cache
+        if c is None or c["names"] is not names:
+            ends = np.asarray([self._tasks_all[nm] for nm in names], dtype=np.int64).reshape(n, 2)
+            r = ends % self.plane
+            y, x = np.divmod(r, self.nx)
+            dist = np.abs(x[:, 1] - x[:, 0]) + np.abs(y[:, 1] - y[:, 0])
+            full = (dist >= ROI_THRESHOLD_STEPS).astype(np.int32)
+            c = self._table_cache = dict(
+                names=names, dist=dist, full_host=full.astype(np.uint8), bonus=None, nids=-1,
+                src=torch.from_numpy(ends[:, 0].astype(np.int32)).to(dev),
+                dst=torch.from_numpy(ends[:, 1].astype(np.int32)).to(dev),
+                full=torch.from_numpy(full).to(dev))
+        if c["nids"] != len(self.net_id_map):
+            nid = np.fromiter((self._net_id(nm) for nm in names), dtype=np.int32, count=n)
+            c["id"] = torch.from_numpy(nid).to(dev)
+            c["nids"] = len(self.net_id_map)
+        if c["bonus"] != bonus:
+            depth = np.empty(2 * n, dtype=np.int32)
+            halo = np.empty(2 * n, dtype=np.int32)
+            for j, b in enumerate((bonus, bonus * 2)):
+                radius = np.maximum(60, np.trunc(c["dist"] * 0.75 + b * 2.0).astype(np.int64))
+                depth[j::2] = np.minimum(np.trunc(radius + b * 2.0).astype(np.int64), 80)
+                halo[j::2] = min(16, 2 + int(max(0.0, b) / 0.6))
+            c["depth"] = torch.from_numpy(depth).to(dev)
+            c["halo"] = torch.from_numpy(halo).to(dev)
+            c["bonus"] = bonus
+        return {k: c[k] for k in ("src", "dst", "id", "full", "depth", "halo", "full_host")}
 
     def _route_all_pass(self, tasks, all_tasks, ordered, bonus, live):
         """The per-net loop of ``_route_all`` as one device launch."""
@@ -1285,15 +1316,16 @@ class PathFinderRouter:
             self.ops.counters["h2d_bytes"] += 16 * len(order)
         self.ops.counters["d2h_bytes"] += 4 * lengths.size + 4 * tot
         paths = self._net_paths
+        olds, news = [], []
         for k, name in enumerate(ordered):
             old = paths.get(name)
             if old:
-                self._mark_nodes(name, old, -1, paths.array(name))
+                olds.append(paths.array(name))
                 self._clear_tracking(name)
             n = int(lens[k])
             if n >= 2:
                 arr = packed[offs[k]:offs[k] + n].astype(np.int64)
-                self._mark_nodes(name, None, +1, arr)
+                news.append(arr)
                 paths.set_path(name, arr.tolist(), arr)
                 self._update_tracking(name, 2 * (n - 1))
             else:
@@ -1301,6 +1333,10 @@ class PathFinderRouter:
                 self._clear_tracking(name)
             if self.search_log is not None:
                 self.search_log.append((self.iteration, name, "pass", self.net_paths[name] or None))
+        # path-node use: every old path off, every new path on (the counts are
+        # exact, so the order of the per-net updates does not matter)
+        self._mark_many(olds, -1)
+        self._mark_many(news, +1)
         routed = sum(1 for p in self.net_paths.values() if p)
         return routed, len(all_tasks) - routed
 
@@ -1652,6 +1688,8 @@ class PathFinderRouter:
         self._task_names = list(tasks)
         self._task_index = {n: i for i, n in enumerate(self._task_names)}
         self._barrel_ids = None              # the store slots' net ids, rebuilt for this job
+        self._table_cache = None             # the pass's per-net parameters, rebuilt for this job
+        self._dist3 = None
         if self.mode == "persistent":
             if self.store is None or self.store.num_nets != len(tasks):
                 self.store = PathStore(self.g, len(tasks),

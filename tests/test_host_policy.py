@@ -365,3 +365,22 @@ def test_barrel_lists_from_the_device_give_the_host_result(seed):
             ns.mark_use(p)
     want, info = detect_barrel_conflicts(esrc, edst, ns, paths, edges, h.net_id_map, h.iteration)
     assert dev[0] == want and dev[4] == info["exact_pairs"] and dev[3] == info["conflict_nets"]
+
+
+def test_batched_node_use_marks_equal_per_path_marks():
+    """The pass epilogue marks every old path off and every new path on in one
+    batch each; a path's distinct nodes count once, as _mark_nodes counts them."""
+    rng = np.random.default_rng(5)
+    a, b = _router(), _router()
+    paths = [rng.integers(0, a.N, size=int(rng.integers(1, 40))).astype(np.int64) for _ in range(50)]
+    paths.append(np.asarray([3, 3, 7, 3], dtype=np.int64))          # repeated nodes count once
+    for p in paths:
+        a._mark_nodes("x", None, +1, p)
+    b._mark_many(paths, +1)
+    np.testing.assert_array_equal(a.node_use, b.node_use)
+    off = paths[::3]
+    for p in off:
+        a._mark_nodes("x", None, -1, p)
+    b._mark_many(off, -1)
+    np.testing.assert_array_equal(a.node_use, b.node_use)
+    assert a.node_use.min() >= 0 and a.node_use.sum() > 0
