@@ -384,3 +384,36 @@ def test_batched_node_use_marks_equal_per_path_marks():
     b._mark_many(off, -1)
     np.testing.assert_array_equal(a.node_use, b.node_use)
     assert a.node_use.min() >= 0 and a.node_use.sum() > 0
+
+
+def test_net_table_cache_equals_the_per_pass_loop():
+    """The per-net search parameters (_net_table, extract_roi :2240-2255): the
+    cached and vectorised table equals the per-net formula for every
+    stagnation bonus, and net ids keep their first-use order (this pass's
+    order first, then task order)."""
+    rng = np.random.default_rng(8)
+    h = _router(nx=300, ny=200, nz=4)
+    names = [f"N{i}" for i in range(60)]
+    h._tasks_all = {n: (int(rng.integers(0, h.plane)), int(rng.integers(0, h.plane))) for n in names}
+    h._task_names = list(names)
+    h._table_cache = None
+    ordered = names[::-1][:20]                      # this pass routes 20 nets, in reverse order
+    for n in ordered:
+        h._net_id(n)
+    for bonus in (0.0, 0.0, 0.6, 3.0, 0.6):
+        t = h._net_table(bonus)
+        for i, n in enumerate(names):
+            s_, d_ = h._tasks_all[n]
+            dist = h._manhattan(s_, d_)
+            assert int(t["src"][i]) == s_ and int(t["dst"][i]) == d_
+            assert int(t["full"][i]) == (1 if dist >= R.ROI_THRESHOLD_STEPS else 0) == int(t["full_host"][i])
+            assert int(t["id"][i]) == h.net_id_map[n]
+            for j, b in enumerate((bonus, bonus * 2)):
+                radius = max(60, int(dist * 0.75 + b * 2.0))
+                assert int(t["depth"][2 * i + j]) == min(int(radius + b * 2.0), 80)
+                assert int(t["halo"][2 * i + j]) == min(16, 2 + int(max(0.0, b) / 0.6))
+    # ids: the pass's nets in its order, then the rest in task order
+    want = {n: k for k, n in enumerate(ordered)}
+    for n in names:
+        want.setdefault(n, len(want))
+    assert h.net_id_map == want
