@@ -32,7 +32,7 @@ def _worker(rank, world, port, out):
 
 def test_replica_max_over_two_gloo_ranks():
     world = 2
-    mgr = mp.Manager()
+    mgr = mp.get_context("spawn").Manager()      # no fork of a process that already runs threads
     out = mgr.dict()
     mp.spawn(_worker, args=(world, _free_port(), out), nprocs=world, join=True)
     assert out[0] == out[1] == (1500.0, pytest.approx(0.75))
