@@ -3,8 +3,9 @@
 * c0 (100x100x6, 200 nets, 10 iterations) is routed by the GPU router and by
   the CPU oracle loop in the same process: every iteration's paths, the
   metrics and the final tallies must be identical.
-* c0 and c1 (600x400x12, 2,000 nets, 40 iterations) are compared with the
-  oracle trajectories committed under ``tests/golden`` (written by
+* c0, c1 (600x400x12, 2,000 nets, 40 iterations) and c2 (the same lattice,
+  4,135 multi-pin star requests) are compared with the oracle trajectories
+  committed under ``tests/golden`` (written by
   ``tests/golden/make_c1_trajectory.py``; c1 takes hours on the CPU).  Those
   runs fixed ``PYTHONHASHSEED`` (the detail pass picks nets in string-hash
   order), so the GPU job runs in a child process with the same seed.
@@ -119,3 +120,17 @@ def test_c1_matches_committed_oracle_trajectory():
     want = load(path)
     got = run_child("c1", seed=want["pythonhashseed"] or "0")
     compare_with_fixture(got, want)
+
+
+def test_c2_matches_committed_oracle_trajectory():
+    """The multi-pin workload: all 40 iterations of 1,500 nets as 4,135 star
+    requests (every one an ROI net, batched in disjoint windows) against the
+    oracle's run."""
+    from orthoroute_gb300.trajectory import load
+    path = os.path.join(G, "c2_trajectory.json.gz")
+    if not os.path.exists(path):
+        pytest.skip("c2 oracle trajectory not generated")
+    want = load(path)
+    got = run_child("c2", seed=want["pythonhashseed"] or "0")
+    compare_with_fixture(got, want)
+
